@@ -1,0 +1,17 @@
+"""GB300-native transfer hot path of FlowInvariantTransfer.jl (imported as ``fit_gb300``).
+
+Python host mirror of the reference API over libfit_gb300.so (hand-written CUDA for sm_103a):
+the pseudospectral nonlinear term with 2/3 or 3/2 dealiasing and the shell-binned reductions
+built on it — spectral flux, shell-to-shell, partial fluxes, mode-to-mode.
+"""
+from .types import *  # noqa: F401,F403
+from .shells import (wavenumber_grid, shell_edges, shell_centers, n_shells, default_binning, kmax,  # noqa: F401
+                     dims_mask)
+from .api import (compute_nonlinear_term, transfer_density, decompose_field, assign_shells_device,  # noqa: F401
+                  calculate_spectral_flux, calculate_scalar_flux, calculate_shell_to_shell_transfer,
+                  calculate_scalar_shell_to_shell_transfer, calculate_partial_fluxes,
+                  calculate_helical_partial_fluxes, calculate_mode_to_mode_transfer,
+                  calculate_scalar_mode_to_mode_transfer, calculate_energy_transfer)
+from .plan import Plan, get_plan, clear_plans  # noqa: F401
+from . import _lib  # noqa: F401
+from ._lib import FitError, launch_count, lib_path  # noqa: F401

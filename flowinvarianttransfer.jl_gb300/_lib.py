@@ -1,0 +1,88 @@
+"""ctypes binding of libfit_gb300.so (the C ABI in include/fit_gb300.h).
+
+The library is the only compute path: there is no CPU fallback, and loading fails loudly when the
+shared object is missing or does not export every declared entry point."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+EXPORTS = [
+    "fit_plan_create", "fit_plan_destroy", "fit_last_error", "fit_plan_set_stream", "fit_plan_info",
+    "fit_launch_count", "fit_nonlinear_term", "fit_assign_shells", "fit_transfer_density",
+    "fit_spectral_flux", "fit_shell_to_shell", "fit_helical_decompose", "fit_helmholtz_decompose",
+    "fit_partial_fluxes", "fit_mode_to_mode",
+]
+
+PTR_HOST, PTR_DEVICE = 0, 1
+DEALIAS = {"none": 0, "two_thirds": 1, "three_halves": 2}
+S2S_PLAIN, S2S_BATCHED = 0, 1
+ERRORS = {-1: "argument", -2: "size", -3: "cuda", -4: "allocation", -5: "state"}
+
+_lib = None
+
+
+class FitError(RuntimeError):
+    """A failure inside libfit_gb300 (CUDA, allocation or state)."""
+
+
+def _declare(lib):
+    vp, i32, i64, u32, dp = C.c_void_p, C.c_int, C.c_int64, C.c_uint32, C.POINTER(C.c_double)
+    lib.fit_plan_create.argtypes = [C.POINTER(vp), i32, C.POINTER(i64), i32, i32, i32, i32, i32, C.POINTER(dp)]
+    lib.fit_plan_destroy.argtypes = [vp]
+    lib.fit_last_error.restype = C.c_char_p
+    lib.fit_last_error.argtypes = []
+    lib.fit_plan_set_stream.argtypes = [vp, vp]
+    lib.fit_plan_info.argtypes = [vp, C.POINTER(i64), i32]
+    lib.fit_launch_count.restype = C.c_longlong
+    lib.fit_launch_count.argtypes = []
+    lib.fit_nonlinear_term.argtypes = [vp, vp, vp, vp, i32]
+    lib.fit_assign_shells.argtypes = [vp, dp, i32, u32, i32, vp, i32]
+    lib.fit_transfer_density.argtypes = [vp, i32, vp, vp, vp, i32]
+    lib.fit_spectral_flux.argtypes = [vp, vp, vp, vp, dp, i32, u32, i32, i32, vp, vp, i32]
+    lib.fit_shell_to_shell.argtypes = [vp, vp, vp, dp, i32, u32, i32, i32, i32, i32, vp, vp, vp, i32]
+    lib.fit_helical_decompose.argtypes = [vp, vp, vp, vp, i32]
+    lib.fit_helmholtz_decompose.argtypes = [vp, vp, vp, vp, i32]
+    lib.fit_partial_fluxes.argtypes = [vp, vp, i32, i32, dp, i32, u32, i32, vp, i32]
+    lib.fit_mode_to_mode.argtypes = [vp, vp, vp, i32, i32, vp, vp, i32]
+    for name in EXPORTS:
+        if name not in ("fit_last_error", "fit_launch_count"):
+            getattr(lib, name).restype = C.c_int
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the shared library; raises if any export is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise FitError(f"libfit_gb300.so not found at {path}; run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    missing = [n for n in EXPORTS if not hasattr(lib, n)]
+    if missing:
+        raise FitError(f"libfit_gb300.so lacks exports {missing}")
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc == 0:
+        return
+    msg = _lib.fit_last_error().decode(errors="replace")
+    if rc in (-1, -2):
+        raise ValueError(msg)
+    raise FitError(f"libfit_gb300 {ERRORS.get(rc, rc)} error: {msg}")
+
+
+def launch_count() -> int:
+    return int(load().fit_launch_count())

@@ -1,0 +1,92 @@
+// Shared definitions for libfit_gb300: complex helpers, error plumbing, launch bookkeeping.
+//
+// Conventions (same as FlowInvariantTransfer.jl, src/Workspaces.jl:46-75):
+//   * user arrays are column-major (ns..., comp), interleaved complex (ComplexF64 / ComplexF32);
+//   * wavenumbers are FFTW-order with +N/2 at the Nyquist index (src/Utils.jl:51-63).
+// Internally every transform runs on a half spectrum along x (kx in [0, M0/2]) of the transform
+// grid M (M = N, or the 3/2-padded grid). A half-spectrum field is stored (Mh0, M1, M2)
+// column-major, Mh0 = M0/2 + 1; a physical field is (M0, M1, M2) real.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#define FIT_OK 0
+#define FIT_ERR_ARG -1
+#define FIT_ERR_SIZE -2
+#define FIT_ERR_CUDA -3
+#define FIT_ERR_ALLOC -4
+#define FIT_ERR_STATE -5
+
+#define FIT_HD __host__ __device__ __forceinline__
+#define FIT_D __device__ __forceinline__
+
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { typedef float2 t; };
+template <> struct Vec2<double> { typedef double2 t; };
+
+template <typename V> struct Scal;
+template <> struct Scal<float2> { typedef float t; };
+template <> struct Scal<double2> { typedef double t; };
+
+template <typename V> FIT_HD V mkc(typename Scal<V>::t x, typename Scal<V>::t y) { V r; r.x = x; r.y = y; return r; }
+template <typename V> FIT_HD V cadd(V a, V b) { return mkc<V>(a.x + b.x, a.y + b.y); }
+template <typename V> FIT_HD V csub(V a, V b) { return mkc<V>(a.x - b.x, a.y - b.y); }
+template <typename V> FIT_HD V cmul(V a, V b) { return mkc<V>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <typename V> FIT_HD V cconj(V a) { return mkc<V>(a.x, -a.y); }
+template <typename V, typename S> FIT_HD V cscale(V a, S s) { return mkc<V>(a.x * s, a.y * s); }
+// multiply by +i (POS) or -i
+template <typename V, bool POS> FIT_HD V cmuli(V a) { return POS ? mkc<V>(-a.y, a.x) : mkc<V>(a.y, -a.x); }
+
+// Thread-local error string for fit_last_error().
+void fit_set_error(const char* fmt, ...);
+const char* fit_get_error();
+
+// Every launch of a library kernel is counted (graph replays add the kernels they contain).
+void fit_count_launches(long n);
+long fit_launch_total();
+
+#define FIT_CUDA_CHECK(expr)                                                                 \
+  do {                                                                                     \
+    cudaError_t _e = (expr);                                                               \
+    if (_e != cudaSuccess) {                                                               \
+      fit_set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return FIT_ERR_CUDA;                                                                 \
+    }                                                                                      \
+  } while (0)
+
+#define FIT_LAUNCH_CHECK()                                                                   \
+  do {                                                                                     \
+    cudaError_t _e = cudaGetLastError();                                                   \
+    if (_e != cudaSuccess) {                                                               \
+      fit_set_error("kernel launch failed: %s (%s:%d)", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return FIT_ERR_CUDA;                                                                 \
+    }                                                                                      \
+    fit_count_launches(1);                                                                 \
+  } while (0)
+
+#define FIT_TRY(expr)            \
+  do {                           \
+    int _rc = (expr);            \
+    if (_rc != FIT_OK) return _rc; \
+  } while (0)
+
+// Radix schedule of one transform length (product of the entries = N).
+struct Radices {
+  int n;
+  int r[16];
+};
+
+// Geometry of the transform grid and its relation to the user grid.
+//   N: user (data) grid; M: transform grid (M == N unless padded); Mh0 = M0/2 + 1.
+struct GridDesc {
+  int nd;
+  int N[3];
+  int M[3];
+  int Mh0;
+  int padded;     // 1 for the 3/2 path
+  long Ntot;      // prod N
+  long Mtot;      // prod M (physical points)
+  long Mhalf;     // Mh0 * M1 * M2 (half-spectrum modes)
+};

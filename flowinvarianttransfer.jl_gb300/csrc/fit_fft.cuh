@@ -1,0 +1,290 @@
+// Shared-memory Stockham FFT engine (radix 2/3/4/5/8, FP32 or FP64) and its pass kernels.
+//
+// One CTA transforms a tile of C lines at once. The tile lives in shared memory as
+// [element][column] with an XOR swizzle on the column (element e of column c at
+// e*C + (c ^ (e & (C-1)))), so that both access shapes used here are bank-conflict free:
+// lanes running along columns (strided passes, every butterfly stage) and lanes running along
+// elements (the x-pass loads/stores of contiguous lines).
+//
+// Stage s of radix r, current span Ns (product of the radices before it), butterfly j:
+//   inputs  x[j + q*N/r] (q < r), twiddled by w^{(j mod Ns) * q * N/(Ns*r)}, w = e^{-+2 pi i/N};
+//   outputs y[q] of the radix-r DFT go to (j div Ns)*Ns*r + (j mod Ns) + q*Ns.
+// This is the self-sorting (autosort) Stockham formulation: after the last stage the line is
+// in natural order. All reads of a stage complete (barrier) before its writes, so one buffer
+// suffices. Twiddles come from an FP64 host table (no device trigonometry).
+#pragma once
+
+#include "fit_common.cuh"
+
+namespace fit {
+
+FIT_D int swz(int e, int c, int C) { return e * C + (c ^ (e & (C - 1))); }
+
+// ---- radix-r DFTs in registers; INV selects e^{+2 pi i/r} --------------------------------------
+
+template <typename V, bool INV>
+FIT_D void dft2(V* v) {
+  V t = v[0];
+  v[0] = cadd(t, v[1]);
+  v[1] = csub(t, v[1]);
+}
+
+template <typename V, bool INV>
+FIT_D void dft4(V* v) {
+  V t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  V t2 = cadd(v[1], v[3]), t3 = cmuli<V, INV>(csub(v[1], v[3]));
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[3] = csub(t1, t3);
+}
+
+template <typename V, bool INV>
+FIT_D void dft8(V* v) {
+  typedef typename Scal<V>::t S;
+  const S h = (S)0.70710678118654752440;
+  V a[4], b[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    a[q] = cadd(v[q], v[q + 4]);
+    b[q] = csub(v[q], v[q + 4]);
+  }
+  // b[q] *= w^q, w = e^{-+2 pi i/8}
+  if (!INV) {
+    b[1] = mkc<V>((b[1].x + b[1].y) * h, (b[1].y - b[1].x) * h);
+    b[3] = mkc<V>((b[3].y - b[3].x) * h, -(b[3].x + b[3].y) * h);
+  } else {
+    b[1] = mkc<V>((b[1].x - b[1].y) * h, (b[1].x + b[1].y) * h);
+    b[3] = mkc<V>(-(b[3].x + b[3].y) * h, (b[3].x - b[3].y) * h);
+  }
+  b[2] = cmuli<V, INV>(b[2]);
+  dft4<V, INV>(a);
+  dft4<V, INV>(b);
+  v[0] = a[0]; v[2] = a[1]; v[4] = a[2]; v[6] = a[3];
+  v[1] = b[0]; v[3] = b[1]; v[5] = b[2]; v[7] = b[3];
+}
+
+template <typename V, bool INV>
+FIT_D void dft3(V* v) {
+  typedef typename Scal<V>::t S;
+  const S s3 = (S)0.86602540378443864676;
+  V t1 = cadd(v[1], v[2]);
+  V t2 = csub(v[1], v[2]);
+  V m = csub(v[0], cscale(t1, (S)0.5));
+  V u = cscale(cmuli<V, INV>(t2), s3);
+  v[0] = cadd(v[0], t1);
+  v[1] = cadd(m, u);
+  v[2] = csub(m, u);
+}
+
+template <typename V, bool INV>
+FIT_D void dft5(V* v) {
+  typedef typename Scal<V>::t S;
+  const S c1 = (S)0.30901699437494742410, c2 = (S)-0.80901699437494742410;
+  const S s1 = (S)0.95105651629515357212, s2 = (S)0.58778525229247312917;
+  V t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+  V t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+  V a1 = cadd(v[0], cadd(cscale(t1, c1), cscale(t2, c2)));
+  V a2 = cadd(v[0], cadd(cscale(t1, c2), cscale(t2, c1)));
+  V u1 = cmuli<V, INV>(cadd(cscale(t3, s1), cscale(t4, s2)));
+  V u2 = cmuli<V, INV>(csub(cscale(t3, s2), cscale(t4, s1)));
+  v[0] = cadd(v[0], cadd(t1, t2));
+  v[1] = cadd(a1, u1);
+  v[4] = csub(a1, u1);
+  v[2] = cadd(a2, u2);
+  v[3] = csub(a2, u2);
+}
+
+template <typename V, int R, bool INV>
+FIT_D void dftr(V* v) {
+  if (R == 2) dft2<V, INV>(v);
+  else if (R == 3) dft3<V, INV>(v);
+  else if (R == 4) dft4<V, INV>(v);
+  else if (R == 5) dft5<V, INV>(v);
+  else dft8<V, INV>(v);
+}
+
+// One in-place Stockham stage over a C-column tile. EPT = tile elements per thread.
+template <typename V, int R, bool INV, int EPT>
+__device__ __forceinline__ void stage(V* s, int N, int C, int Ns, const V* tw, int tid, int nthr) {
+  constexpr int MAXB = (EPT + R - 1) / R;
+  const int NR = N / R;
+  const int nb = C * NR;
+  const int tstride = N / (Ns * R);
+  V v[MAXB][R];
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = tid + i * nthr;
+    if (b < nb) {
+      const int c = b & (C - 1);
+      const int j = b / C;
+      const int k = j % Ns;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        V x = s[swz(j + q * NR, c, C)];
+        if (q > 0 && k > 0) {
+          V w = tw[k * q * tstride];
+          if (INV) w.y = -w.y;
+          x = cmul(x, w);
+        }
+        v[i][q] = x;
+      }
+      dftr<V, R, INV>(v[i]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = tid + i * nthr;
+    if (b < nb) {
+      const int c = b & (C - 1);
+      const int j = b / C;
+      const int k = j % Ns;
+      const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) s[swz(base + q * Ns, c, C)] = v[i][q];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename V, bool INV, int EPT>
+__device__ __forceinline__ void fft_smem(V* s, int N, int C, const Radices& rd, const V* tw, int tid,
+                                         int nthr) {
+  int Ns = 1;
+  for (int st = 0; st < rd.n; ++st) {
+    const int r = rd.r[st];
+    switch (r) {
+      case 8: stage<V, 8, INV, EPT>(s, N, C, Ns, tw, tid, nthr); break;
+      case 4: stage<V, 4, INV, EPT>(s, N, C, Ns, tw, tid, nthr); break;
+      case 2: stage<V, 2, INV, EPT>(s, N, C, Ns, tw, tid, nthr); break;
+      case 3: stage<V, 3, INV, EPT>(s, N, C, Ns, tw, tid, nthr); break;
+      default: stage<V, 5, INV, EPT>(s, N, C, Ns, tw, tid, nthr); break;
+    }
+    Ns *= r;
+  }
+}
+
+template <typename V>
+FIT_D void load_twiddles(V* tw, const V* __restrict__ twg, int N, int tid, int nthr) {
+  for (int t = tid; t < N; t += nthr) tw[t] = twg[t];
+}
+
+// ---- pass kernels ---------------------------------------------------------------------------
+
+// Complex transform along a strided axis. Lines are indexed by (column, q): line element e of
+// column col lives at  q*P*N + col + e*P  (P = product of the faster dimensions). Tiles cover C
+// consecutive columns of one q. In-place use (in == out) is safe: a CTA reads its whole tile
+// before writing it.
+template <typename V, bool INV, int EPT>
+__global__ void __launch_bounds__(1024) k_pass_strided(const V* in, V* out, int N, long P, long tilesPerQ,
+                                                      int C, Radices rd, const V* __restrict__ twg,
+                                                      typename Scal<V>::t scale) {
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + (size_t)C * N;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const long tile = blockIdx.x;
+  const long q = tile / tilesPerQ;
+  const long c0 = (tile - q * tilesPerQ) * C;
+  const long base = q * P * (long)N;
+  const int E = C * N;
+  load_twiddles(tw, twg, N, tid, nthr);
+  for (int i = tid; i < E; i += nthr) {
+    const int c = i & (C - 1), e = i / C;
+    const long col = c0 + c;
+    V x = mkc<V>(0, 0);
+    if (col < P) x = in[base + col + (long)e * P];
+    s[swz(e, c, C)] = x;
+  }
+  __syncthreads();
+  fft_smem<V, INV, EPT>(s, N, C, rd, tw, tid, nthr);
+  for (int i = tid; i < E; i += nthr) {
+    const int c = i & (C - 1), e = i / C;
+    const long col = c0 + c;
+    if (col < P) out[base + col + (long)e * P] = cscale(s[swz(e, c, C)], scale);
+  }
+}
+
+// Inverse real transform along x: L half-spectrum lines (N/2+1 complex, contiguous) -> L real
+// lines (N, contiguous). Two real lines share one complex transform: Z = A + iB, where A, B are
+// the Hermitian extensions of lines 2c and 2c+1; the imaginary parts of the self-conjugate
+// bins (k = 0, k = N/2) are dropped, which is what real(ifft(.)) keeps.
+template <typename V, int EPT>
+__global__ void __launch_bounds__(1024) k_c2r_x(const V* __restrict__ in, typename Scal<V>::t* __restrict__ out,
+                                                int N, long L, int C, Radices rd, const V* __restrict__ twg,
+                                                typename Scal<V>::t scale) {
+  typedef typename Scal<V>::t S;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + (size_t)C * N;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int Nh = N / 2 + 1;
+  const long l0 = (long)blockIdx.x * 2 * C;
+  const int E = C * N;
+  load_twiddles(tw, twg, N, tid, nthr);
+  for (int i = tid; i < E; i += nthr) {
+    const int c = i / N, k = i - c * N;
+    const long a = l0 + 2 * c, b = a + 1;
+    const bool cj = 2 * k > N;
+    const int kk = cj ? N - k : k;
+    const bool selfc = (k == 0) || (2 * k == N);
+    V A = mkc<V>(0, 0), B = mkc<V>(0, 0);
+    if (a < L) {
+      A = in[a * Nh + kk];
+      if (cj) A.y = -A.y;
+      if (selfc) A.y = 0;
+    }
+    if (b < L) {
+      B = in[b * Nh + kk];
+      if (cj) B.y = -B.y;
+      if (selfc) B.y = 0;
+    }
+    s[swz(k, c, C)] = mkc<V>(A.x - B.y, A.y + B.x);
+  }
+  __syncthreads();
+  fft_smem<V, true, EPT>(s, N, C, rd, tw, tid, nthr);
+  for (int i = tid; i < E; i += nthr) {
+    const int c = i / N, x = i - c * N;
+    const long a = l0 + 2 * c, b = a + 1;
+    const V z = s[swz(x, c, C)];
+    if (a < L) out[a * N + x] = z.x * scale;
+    if (b < L) out[b * N + x] = z.y * scale;
+  }
+}
+
+// Forward real transform along x: L real lines -> L half-spectrum lines (two-for-one packing).
+template <typename V, int EPT>
+__global__ void __launch_bounds__(1024) k_r2c_x(const typename Scal<V>::t* __restrict__ in, V* __restrict__ out,
+                                                int N, long L, int C, Radices rd, const V* __restrict__ twg,
+                                                typename Scal<V>::t scale) {
+  typedef typename Scal<V>::t S;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + (size_t)C * N;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int Nh = N / 2 + 1;
+  const long l0 = (long)blockIdx.x * 2 * C;
+  const int E = C * N;
+  load_twiddles(tw, twg, N, tid, nthr);
+  for (int i = tid; i < E; i += nthr) {
+    const int c = i / N, x = i - c * N;
+    const long a = l0 + 2 * c, b = a + 1;
+    const S ra = (a < L) ? in[a * N + x] : (S)0;
+    const S rb = (b < L) ? in[b * N + x] : (S)0;
+    s[swz(x, c, C)] = mkc<V>(ra, rb);
+  }
+  __syncthreads();
+  fft_smem<V, false, EPT>(s, N, C, rd, tw, tid, nthr);
+  const S hs = (S)0.5 * scale;
+  for (int i = tid; i < C * Nh; i += nthr) {
+    const int c = i / Nh, k = i - c * Nh;
+    const long a = l0 + 2 * c, b = a + 1;
+    const V zk = s[swz(k, c, C)];
+    const V zn = s[swz(k == 0 ? 0 : N - k, c, C)];
+    if (a < L) out[a * Nh + k] = mkc<V>((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+    if (b < L) out[b * Nh + k] = mkc<V>((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+  }
+}
+
+}  // namespace fit

@@ -1,0 +1,236 @@
+// Host launchers of the Stockham pass kernels: tile selection, twiddle tables, n-D transforms.
+#include <math.h>
+#include <stdlib.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "fit_fft.cuh"
+#include "fit_ops.cuh"
+
+namespace fit {
+
+int axis_init(Axis* a, int N) {
+  a->N = N;
+  a->tw32 = nullptr;
+  a->tw64 = nullptr;
+  if (N < 1) {
+    fit_set_error("transform length %d must be positive", N);
+    return FIT_ERR_SIZE;
+  }
+  int n = N, p2 = 0, ns = 0;
+  while (n % 2 == 0) { n /= 2; ++p2; }
+  int n3 = 0, n5 = 0;
+  while (n % 3 == 0) { n /= 3; ++n3; }
+  while (n % 5 == 0) { n /= 5; ++n5; }
+  if (n != 1) {
+    fit_set_error("transform length %d has a prime factor other than 2, 3, 5 (unsupported)", N);
+    return FIT_ERR_SIZE;
+  }
+  Radices rd;
+  for (int i = 0; i < p2 / 3; ++i) rd.r[ns++] = 8;
+  if (p2 % 3 == 2) rd.r[ns++] = 4;
+  if (p2 % 3 == 1) rd.r[ns++] = 2;
+  for (int i = 0; i < n3; ++i) rd.r[ns++] = 3;
+  for (int i = 0; i < n5; ++i) rd.r[ns++] = 5;
+  if (ns > 16) {
+    fit_set_error("transform length %d needs too many radix stages", N);
+    return FIT_ERR_SIZE;
+  }
+  rd.n = ns;
+  a->rd = rd;
+  double2* h64 = (double2*)malloc(sizeof(double2) * N);
+  float2* h32 = (float2*)malloc(sizeof(float2) * N);
+  if (!h64 || !h32) {
+    free(h64);
+    free(h32);
+    fit_set_error("host allocation failed");
+    return FIT_ERR_ALLOC;
+  }
+  for (int t = 0; t < N; ++t) {
+    // exact symmetric evaluation: reduce to the first octant-free form via long double
+    long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)t / (long double)N;
+    double c = (double)cosl(ang), s = (double)sinl(ang);
+    if (4 * t == N) { c = 0.0; s = -1.0; }
+    if (2 * t == N) { c = -1.0; s = 0.0; }
+    if (4 * t == 3 * N) { c = 0.0; s = 1.0; }
+    h64[t] = make_double2(c, s);
+    h32[t] = make_float2((float)c, (float)s);
+  }
+  cudaError_t e1 = cudaMalloc(&a->tw64, sizeof(double2) * N);
+  cudaError_t e2 = cudaMalloc(&a->tw32, sizeof(float2) * N);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    free(h64);
+    free(h32);
+    fit_set_error("cudaMalloc of twiddle tables failed");
+    return FIT_ERR_ALLOC;
+  }
+  cudaError_t e3 = cudaMemcpy(a->tw64, h64, sizeof(double2) * N, cudaMemcpyHostToDevice);
+  cudaError_t e4 = cudaMemcpy(a->tw32, h32, sizeof(float2) * N, cudaMemcpyHostToDevice);
+  free(h64);
+  free(h32);
+  if (e3 != cudaSuccess || e4 != cudaSuccess) {
+    fit_set_error("twiddle upload failed");
+    return FIT_ERR_CUDA;
+  }
+  return FIT_OK;
+}
+
+void axis_free(Axis* a) {
+  if (a->tw32) cudaFree(a->tw32);
+  if (a->tw64) cudaFree(a->tw64);
+  a->tw32 = nullptr;
+  a->tw64 = nullptr;
+}
+
+struct Tile {
+  int C, EPT, nthr;
+  size_t smem;
+};
+
+// Columns per CTA: full 128-byte rows, ~64 KB of tile data (at most 128 KB), never more columns
+// than exist. Elements per thread: 8 (<= 8192 elements) or 16.
+static Tile pick_tile(int N, int vbytes, long avail_cols) {
+  const int Cmin = 128 / vbytes;
+  const long Emax = 131072 / vbytes;
+  const long Etar = 65536 / vbytes;
+  int C = 1;
+  while ((long)C * N < Etar) C *= 2;
+  if (C < Cmin) C = Cmin;
+  while (C > 1 && (long)C * N > Emax) C /= 2;
+  long ap2 = 1;
+  while (ap2 < avail_cols) ap2 *= 2;
+  if (C > ap2) C = (int)ap2;
+  const long E = (long)C * N;
+  Tile t;
+  t.C = C;
+  t.EPT = (E <= 8192) ? 8 : 16;
+  long nthr = (E + t.EPT - 1) / t.EPT;
+  nthr = ((nthr + 31) / 32) * 32;
+  if (nthr < 32) nthr = 32;
+  t.nthr = (int)nthr;
+  t.smem = (size_t)(E + N) * vbytes;
+  return t;
+}
+
+// Raise the dynamic shared-memory limit of a kernel once (the attribute is per function; a
+// cached value keeps the call out of captured launch sequences after the first use).
+template <typename K>
+static int prep_kernel(K kern, size_t smem) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> done;
+  if (smem <= 48 * 1024) return FIT_OK;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = done.find((const void*)kern);
+  if (it != done.end() && it->second >= smem) return FIT_OK;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    fit_set_error("cudaFuncSetAttribute(smem=%zu) failed: %s", smem, cudaGetErrorString(e));
+    return FIT_ERR_CUDA;
+  }
+  done[(const void*)kern] = smem;
+  return FIT_OK;
+}
+
+template <typename T>
+int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const Axis& ax, long P, long Q,
+                 bool inverse, T scale, cudaStream_t st) {
+  typedef typename Vec2<T>::t V;
+  if (P <= 0 || Q <= 0) return FIT_OK;
+  Tile t = pick_tile(ax.N, sizeof(V), P);
+  if (t.nthr > 1024) {
+    fit_set_error("tile too large");
+    return FIT_ERR_SIZE;
+  }
+  const long tpq = (P + t.C - 1) / t.C;
+  const long grid = tpq * Q;
+  if (grid > 2147483647L) {
+    fit_set_error("grid too large");
+    return FIT_ERR_SIZE;
+  }
+  const V* tw = axis_tw<T>(ax);
+#define FIT_PS_LAUNCH(INV, EPT)                                                                          \
+  do {                                                                                                 \
+    FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, t.smem));                                         \
+    k_pass_strided<V, INV, EPT><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, P, tpq, t.C, ax.rd, tw, \
+                                                                          scale);                      \
+  } while (0)
+  if (inverse) {
+    if (t.EPT == 8) FIT_PS_LAUNCH(true, 8); else FIT_PS_LAUNCH(true, 16);
+  } else {
+    if (t.EPT == 8) FIT_PS_LAUNCH(false, 8); else FIT_PS_LAUNCH(false, 16);
+  }
+#undef FIT_PS_LAUNCH
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+template <typename T>
+int pass_c2r_x(const typename Vec2<T>::t* in, T* out, const Axis& ax, long L, T scale, cudaStream_t st) {
+  typedef typename Vec2<T>::t V;
+  if (L <= 0) return FIT_OK;
+  Tile t = pick_tile(ax.N, sizeof(V), (L + 1) / 2);
+  const long grid = (L + 2L * t.C - 1) / (2L * t.C);
+  const V* tw = axis_tw<T>(ax);
+  if (t.EPT == 8) {
+    FIT_TRY(prep_kernel(k_c2r_x<V, 8>, t.smem));
+    k_c2r_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
+  } else {
+    FIT_TRY(prep_kernel(k_c2r_x<V, 16>, t.smem));
+    k_c2r_x<V, 16><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
+  }
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+template <typename T>
+int pass_r2c_x(const T* in, typename Vec2<T>::t* out, const Axis& ax, long L, T scale, cudaStream_t st) {
+  typedef typename Vec2<T>::t V;
+  if (L <= 0) return FIT_OK;
+  Tile t = pick_tile(ax.N, sizeof(V), (L + 1) / 2);
+  const long grid = (L + 2L * t.C - 1) / (2L * t.C);
+  const V* tw = axis_tw<T>(ax);
+  if (t.EPT == 8) {
+    FIT_TRY(prep_kernel(k_r2c_x<V, 8>, t.smem));
+    k_r2c_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
+  } else {
+    FIT_TRY(prep_kernel(k_r2c_x<V, 16>, t.smem));
+    k_r2c_x<V, 16><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
+  }
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+// half (nf fields, destroyed) -> phys (nf fields); x is the last (real) pass.
+template <typename T>
+int inverse_nd(typename Vec2<T>::t* half, T* phys, const GridDesc& g, const Axis* ax, long nf, T scale,
+               cudaStream_t st) {
+  const long Mh0 = g.Mh0, M1 = g.M[1], M2 = g.M[2];
+  if (g.nd == 3) FIT_TRY(pass_strided<T>(half, half, ax[2], Mh0 * M1, nf, true, (T)1, st));
+  if (g.nd >= 2) FIT_TRY(pass_strided<T>(half, half, ax[1], Mh0, M2 * nf, true, (T)1, st));
+  FIT_TRY(pass_c2r_x<T>(half, phys, ax[0], M1 * M2 * nf, scale, st));
+  return FIT_OK;
+}
+
+template <typename T>
+int forward_nd(const T* phys, typename Vec2<T>::t* half, const GridDesc& g, const Axis* ax, long nf, T scale,
+               cudaStream_t st) {
+  const long Mh0 = g.Mh0, M1 = g.M[1], M2 = g.M[2];
+  FIT_TRY(pass_r2c_x<T>(phys, half, ax[0], M1 * M2 * nf, scale, st));
+  if (g.nd >= 2) FIT_TRY(pass_strided<T>(half, half, ax[1], Mh0, M2 * nf, false, (T)1, st));
+  if (g.nd == 3) FIT_TRY(pass_strided<T>(half, half, ax[2], Mh0 * M1, nf, false, (T)1, st));
+  return FIT_OK;
+}
+
+template int pass_strided<float>(const float2*, float2*, const Axis&, long, long, bool, float, cudaStream_t);
+template int pass_strided<double>(const double2*, double2*, const Axis&, long, long, bool, double, cudaStream_t);
+template int pass_c2r_x<float>(const float2*, float*, const Axis&, long, float, cudaStream_t);
+template int pass_c2r_x<double>(const double2*, double*, const Axis&, long, double, cudaStream_t);
+template int pass_r2c_x<float>(const float*, float2*, const Axis&, long, float, cudaStream_t);
+template int pass_r2c_x<double>(const double*, double2*, const Axis&, long, double, cudaStream_t);
+template int inverse_nd<float>(float2*, float*, const GridDesc&, const Axis*, long, float, cudaStream_t);
+template int inverse_nd<double>(double2*, double*, const GridDesc&, const Axis*, long, double, cudaStream_t);
+template int forward_nd<float>(const float*, float2*, const GridDesc&, const Axis*, long, float, cudaStream_t);
+template int forward_nd<double>(const double*, double2*, const GridDesc&, const Axis*, long, double, cudaStream_t);
+
+}  // namespace fit

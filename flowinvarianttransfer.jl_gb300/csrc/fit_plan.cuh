@@ -1,0 +1,55 @@
+// Plan object shared by the C-ABI translation units.
+#pragma once
+
+#include <vector>
+
+#include "fit_ops.cuh"
+
+struct fit_dbuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+struct fit_plan {
+  GridDesc g;
+  int nd = 0;
+  int M = 0;      // advected components
+  int Dadv = 0;   // advecting components
+  int dealias = 0;
+  int prec = 64;
+  int io_f64 = 1;
+  fit::Axis ax[3];
+  int ax_init[3] = {0, 0, 0};
+  std::vector<double> ks_host[3];
+  double* ks_dev[3] = {nullptr, nullptr, nullptr};
+  fit::KTab kt;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  size_t bytes = 0;
+  long buf_gen = 0;   // bumped on every (re)allocation: captured graphs key on it
+
+  // staging copies of host inputs (user layout, io precision)
+  fit_dbuf in_u, in_a, in_c, out_c, out_c2;
+  // generic nonlinear-term workspace
+  fit_dbuf hs, ph, nph, nh;
+  fit_dbuf ceff, seff, partial, outd;
+  // shell table cache
+  fit_dbuf shell_full;
+  fit_dbuf edges_dev;
+  std::vector<double> cached_edges;
+  unsigned cached_dims = 0;
+  int cached_f32 = -1;
+  int nsh = 0;
+  // batched shell-to-shell state (fit_s2s.cu)
+  void* s2s = nullptr;
+};
+
+namespace fit {
+int ensure(fit_plan* p, fit_dbuf* b, size_t bytes);
+int ensure_shells(fit_plan* p, const double* edges, int n_edges, unsigned dims, int coord_f32);
+template <typename T>
+int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u);
+int s2s_batched(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, double* Tdev);
+void s2s_free(fit_plan* p);
+int triad_m2m(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, int fp64, double* S, double* net);
+}  // namespace fit

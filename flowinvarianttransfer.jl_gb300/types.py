@@ -1,0 +1,213 @@
+"""Trait and result types mirroring FlowInvariantTransfer.jl's ``src/Types.jl``.
+
+The names, fields and defaults follow the reference so that calls read the same:
+binnings (``:370-411``), shell geometry (``:506-531``), dealiasing (``:458-476``), invariants
+(``:77-132``), decompositions, spectral / execution backends (``:550-635``) and result structs
+(``:654,719,746``). ``GB300Spectral`` and ``GB300Execution`` are the new backends that route a
+call to the GB300 library.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Any, Optional, Sequence, Tuple
+
+import numpy as np
+
+
+# ---- binning ------------------------------------------------------------------------------------
+class AbstractShellBinning:
+    pass
+
+
+@dataclass(frozen=True)
+class LinearBinning(AbstractShellBinning):
+    dk: float
+
+
+@dataclass(frozen=True)
+class LogarithmicBinning(AbstractShellBinning):
+    k0: float
+    lam: float
+
+
+@dataclass(frozen=True)
+class DyadicBinning(AbstractShellBinning):
+    k0: float = 1.0
+
+
+@dataclass(frozen=True)
+class CustomBinning(AbstractShellBinning):
+    edges: Tuple[float, ...]
+
+    def __init__(self, edges):
+        object.__setattr__(self, "edges", tuple(float(e) for e in edges))
+
+
+# ---- shell geometry -----------------------------------------------------------------------------
+@dataclass(frozen=True)
+class ShellMagnitude:
+    """Bin by sqrt(sum_{d in dims} k_d^2); ``dims=None`` = all axes. dims are 1-based."""
+    dims: Optional[Tuple[int, ...]] = None
+
+
+def IsotropicShells():
+    return ShellMagnitude(None)
+
+
+def PerpendicularShells(dims=(1, 2)):
+    return ShellMagnitude(tuple(dims))
+
+
+def ParallelShells(dims=(3,)):
+    return ShellMagnitude(tuple(dims))
+
+
+# ---- dealiasing ---------------------------------------------------------------------------------
+class AbstractDealiasing:
+    key = ""
+
+
+class NoDealiasing(AbstractDealiasing):
+    key = "none"
+
+
+class OrszagTwoThirds(AbstractDealiasing):
+    key = "two_thirds"
+
+
+class PaddedThreeHalves(AbstractDealiasing):
+    key = "three_halves"
+
+
+# ---- invariants ---------------------------------------------------------------------------------
+class AbstractInvariant:
+    code = -1
+
+
+class KineticEnergy(AbstractInvariant):
+    code = 0
+
+
+class PassiveScalar(AbstractInvariant):
+    code = 1
+
+
+class Helicity(AbstractInvariant):
+    code = 2
+
+
+class Enstrophy(AbstractInvariant):
+    code = 3
+
+
+# ---- decompositions -----------------------------------------------------------------------------
+class AbstractFieldDecomposition:
+    pass
+
+
+class NoDecomposition(AbstractFieldDecomposition):
+    pass
+
+
+class HelicalDecomposition(AbstractFieldDecomposition):
+    names = ("positive", "negative")
+
+
+class HelmholtzDecomposition(AbstractFieldDecomposition):
+    names = ("rotational", "divergent")
+
+
+class RotationalDecomposition(AbstractFieldDecomposition):
+    pass
+
+
+class DivergentDecomposition(AbstractFieldDecomposition):
+    pass
+
+
+# ---- backends -----------------------------------------------------------------------------------
+class AbstractSpectralBackend:
+    pass
+
+
+@dataclass(frozen=True)
+class GB300Spectral(AbstractSpectralBackend):
+    """Transforms and products on the GB300. ``precision`` 64 (the plain FP64 method) or 32
+    (FP32 transforms/products, FP64 reductions); ``None`` follows the input element type."""
+    precision: Optional[int] = None
+
+
+class FFTBackend(AbstractSpectralBackend):
+    """Accepted for drop-in calls: routed to ``GB300Spectral()``."""
+
+
+class DirectSumBackend(AbstractSpectralBackend):
+    """Accepted for drop-in calls: routed to ``GB300Spectral()`` (same arithmetic, O(N log N))."""
+
+
+class AbstractExecutionBackend:
+    pass
+
+
+@dataclass(frozen=True)
+class GB300Execution(AbstractExecutionBackend):
+    """How the shell-to-shell mediator loop runs: ``"batched"`` (mediators batched, fused
+    kernels, CUDA-graph replay) or ``"plain"`` (one nonlinear term per mediator, launched one
+    by one, as the reference's serial loop)."""
+    mode: str = "batched"
+
+
+class SerialBackend(AbstractExecutionBackend):
+    pass
+
+
+class ThreadedBackend(AbstractExecutionBackend):
+    pass
+
+
+# ---- methods (unified dispatch, src/Types.jl) ---------------------------------------------------
+@dataclass(frozen=True)
+class SpectralFluxMethod:
+    binning: AbstractShellBinning
+
+
+@dataclass(frozen=True)
+class ShellToShellTransferMethod:
+    binning: AbstractShellBinning
+
+
+@dataclass(frozen=True)
+class ModeToModeTransferMethod:
+    pass
+
+
+# ---- results ------------------------------------------------------------------------------------
+@dataclass
+class SpectralFluxResult:
+    k_shells: np.ndarray
+    transfer_spectrum: np.ndarray
+    flux: np.ndarray
+
+
+@dataclass
+class ShellToShellResult:
+    shell_centers: np.ndarray
+    shell_edges: np.ndarray
+    transfer_matrix: np.ndarray
+    net_transfer: np.ndarray
+    max_antisymmetry_error: float
+
+
+@dataclass
+class ModeToModeTriadResult:
+    invariant: AbstractInvariant
+    ks: Any
+    net_transfer: np.ndarray
+    transfer: np.ndarray
+
+
+@dataclass
+class PartialFluxResult:
+    channels: dict
+    total: SpectralFluxResult
+    k_shells: np.ndarray

@@ -1,0 +1,132 @@
+/* libfit_gb300 — GB300-native (sm_103a) transfer hot path of FlowInvariantTransfer.jl.
+ *
+ * A thin C ABI (plain pointers and sizes) that a Julia `ccall` binds. Conventions follow the
+ * reference package exactly:
+ *   - spectral arrays are column-major (ns..., comp), interleaved complex: ComplexF64 when the
+ *     plan's io_f64 = 1, ComplexF32 when io_f64 = 0 (src/Workspaces.jl:46-75);
+ *   - wavenumbers ks[d] are FFTW-order vectors with +N/2 at the Nyquist index (src/Utils.jl:51-63);
+ *   - shell edges are passed explicitly (computed by shell_edges, src/ShellBinning.jl:50-79);
+ *     shell indices are Int64, 1-based, 0 = no shell (src/ShellBinning.jl:126-140);
+ *   - T(n,m) is written column-major (n fastest);
+ *   - every real result is FP64 (the caller converts to the input precision when it wants the
+ *     reference's result element type).
+ * ptr_kind: FIT_PTR_HOST (0) = all array arguments are host memory (copied in/out inside the
+ * call); FIT_PTR_DEVICE (1) = all array arguments are device memory. Every call is synchronous
+ * on the plan's stream and returns FIT_OK (0) or a negative error code; fit_last_error() gives
+ * the message (thread-local). Plans are not re-entrant; distinct plans may be used from
+ * distinct threads.
+ */
+#ifndef FIT_GB300_H
+#define FIT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIT_OK 0
+#define FIT_ERR_ARG -1
+#define FIT_ERR_SIZE -2
+#define FIT_ERR_CUDA -3
+#define FIT_ERR_ALLOC -4
+#define FIT_ERR_STATE -5
+
+#define FIT_PTR_HOST 0
+#define FIT_PTR_DEVICE 1
+
+/* dealiasing (src/Types.jl:458-476) */
+#define FIT_DEALIAS_NONE 0
+#define FIT_DEALIAS_TWO_THIRDS 1
+#define FIT_DEALIAS_THREE_HALVES 2
+
+/* invariants (src/Types.jl:77-132) */
+#define FIT_INV_KINETIC_ENERGY 0
+#define FIT_INV_PASSIVE_SCALAR 1
+#define FIT_INV_HELICITY 2
+#define FIT_INV_ENSTROPHY 3
+
+/* decompositions (src/Types.jl) */
+#define FIT_DECOMP_HELICAL 1
+#define FIT_DECOMP_HELMHOLTZ 2
+
+/* shell-to-shell execution forms */
+#define FIT_S2S_PLAIN 0    /* one nonlinear term per mediator shell, launched one by one */
+#define FIT_S2S_BATCHED 1  /* mediators batched, fused kernels, CUDA-graph replay */
+
+typedef struct fit_plan fit_plan;
+
+/* Creates a plan (device buffers, transform tables, one CUDA stream) for fields on grid
+ * ns[0..nd) with n_advected components (M) advected by a velocity of n_advecting (D >= nd)
+ * components. precision = 64 or 32 (arithmetic of the transforms and products; reductions are
+ * always FP64). Replaces the workspace + FFTW plan construction of
+ * ext/FlowInvariantTransferFFTWExt.jl:37-49 (src/Workspaces.jl:22,63-75). */
+int fit_plan_create(fit_plan** out, int nd, const int64_t* ns, int n_advected, int n_advecting, int dealias,
+                    int precision, int io_f64, const double* const* ks);
+int fit_plan_destroy(fit_plan* plan);
+const char* fit_last_error(void);
+/* Use an existing cudaStream_t (passed as void*) instead of the plan's own stream. */
+int fit_plan_set_stream(fit_plan* plan, void* stream);
+/* info[0..7] = nd, N0, N1, N2, M0, M1, M2 (transform grid), bytes of device memory held. */
+int fit_plan_info(const fit_plan* plan, int64_t* info, int n);
+/* Number of library kernels launched since load (graph replays count their kernels). */
+long long fit_launch_count(void);
+
+/* N̂ = FFT[(u_adv·∇) f] in the reference normalisation. Replaces
+ * NonlinearTerm._compute_nonlinear_term! (src/NonlinearTerm.jl:102-116) for the FFT backend:
+ * _nonlinear_term_fft! (ext/FlowInvariantTransferFFTWExt.jl:61-121) and
+ * _nonlinear_term_padded_fft! (:160-183). adv_hat = NULL means self-advection. */
+int fit_nonlinear_term(fit_plan* plan, const void* f_hat, const void* adv_hat, void* N_hat, int ptr_kind);
+
+/* Shell index of every mode. Replaces shell_coordinate + assign_shells
+ * (src/ShellBinning.jl:19-36,126-140). dims_mask bit d selects axis d (all bits = isotropic);
+ * coord_f32 = 1 evaluates the coordinate in Float32 (Float32 wavenumbers). */
+int fit_assign_shells(fit_plan* plan, const double* edges, int n_edges, uint32_t dims_mask, int coord_f32,
+                      int64_t* idx_out, int ptr_kind);
+
+/* Per-mode transfer density t(k) for an invariant. Replaces transfer_density!
+ * (src/Invariants.jl:40-104). N_hat has the plan's n_advected components. */
+int fit_transfer_density(fit_plan* plan, int invariant, const void* carrier, const void* N_hat, double* t_out,
+                         int ptr_kind);
+
+/* T(k_n) and Pi(K_n) = cumsum(T). Replaces calculate_spectral_flux →
+ * _calculate_spectral_flux_with_N̂! (src/SpectralFlux.jl:49-94,148-180). carrier = NULL uses
+ * u_hat (the decomposed-component branch passes the component as carrier, :86-91). */
+int fit_spectral_flux(fit_plan* plan, const void* u_hat, const void* adv_hat, const void* carrier,
+                      const double* edges, int n_edges, uint32_t dims_mask, int coord_f32, int invariant, double* T,
+                      double* Pi, int ptr_kind);
+
+/* Shell-to-shell T(n,m), net transfer and max|T+T'|. Replaces
+ * ShellToShellTransfer._calculate_shell_to_shell! (src/ShellToShell/ShellToShellTransfer.jl:152-159)
+ * → _shell_to_shell_fft! (ext/FlowInvariantTransferFFTWExt.jl:209-295) and the GPU/threaded
+ * execution backends (ext/FlowInvariantTransferKernelAbstractionsExt.jl:68-138,
+ * ext/FlowInvariantTransferOhMyThreadsExt.jl:24-97). mode = FIT_S2S_PLAIN or FIT_S2S_BATCHED.
+ * max_asym receives NaN when verify = 0. */
+int fit_shell_to_shell(fit_plan* plan, const void* u_hat, const void* adv_hat, const double* edges, int n_edges,
+                       uint32_t dims_mask, int coord_f32, int invariant, int mode, int verify, double* T_colmajor,
+                       double* net, double* max_asym, int ptr_kind);
+
+/* Helical (Craya-Herring) split u = u+ + u- (src/Decomposition.jl:63-98). */
+int fit_helical_decompose(fit_plan* plan, const void* u_hat, void* u_plus, void* u_minus, int ptr_kind);
+/* Rotational/divergent split of a 2D field (spectral Leray projection; the reference delegates
+ * to HelmholtzDecomposition.jl, ext/FlowInvariantTransferHelmholtzDecompositionExt.jl:50-104). */
+int fit_helmholtz_decompose(fit_plan* plan, const void* u_hat, void* u_rot, void* u_div, int ptr_kind);
+
+/* Partial fluxes T^{sk,sp,sq}(k_n) of a two-component decomposition (8 channels). Replaces
+ * calculate_partial_fluxes (src/SpectralFlux.jl:240-285); invariant = FIT_INV_HELICITY swaps the
+ * density at :277. T_channels[(sk*4 + sp*2 + sq)*n_shells + n], component 0 = positive /
+ * rotational, 1 = negative / divergent. */
+int fit_partial_fluxes(fit_plan* plan, const void* u_hat, int decomposition, int invariant, const double* edges,
+                       int n_edges, uint32_t dims_mask, int coord_f32, double* T_channels, int ptr_kind);
+
+/* Resolved S(k|p) (column-major [k..., p...]) and net(k) = sum_p S(k|p). Replaces
+ * calculate_mode_to_mode_transfer (src/ScaleToScale/ScaleToScaleTransfer.jl:49-91).
+ * fp64_products = 1 evaluates every triad in FP64, 0 in FP32 with FP64 sums. */
+int fit_mode_to_mode(fit_plan* plan, const void* u_hat, const void* adv_hat, int invariant, int fp64_products,
+                     double* S, double* net, int ptr_kind);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FIT_GB300_H */

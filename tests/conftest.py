@@ -7,6 +7,10 @@ for p in (HERE, ROOT):
     if p not in sys.path:
         sys.path.insert(0, p)
 
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()   # registers the package as ``fit_gb300``
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")

@@ -1,0 +1,223 @@
+"""GPU parity: every entry point of libfit_gb300 against the CPU oracle on seeded inputs.
+
+Tolerances: FP64 plans agree with the FP64 oracle to 1e-12 relative (max-norm over the output);
+FP32 plans (FP32 transforms/products, FP64 reductions) to 1e-5 relative; integer outputs
+(shell indices) bit for bit.
+"""
+import numpy as np
+import pytest
+
+import fit_gb300 as F
+import oracle as O
+from oracle.direct import nonlinear_term_direct
+
+from fields import (curl_noise_3d, e_config1, e_config2, kgrid, scalar_2d, solenoidal_2d, spectrum_field)
+
+pytestmark = pytest.mark.gpu
+
+DEAL = {"none": F.NoDealiasing(), "two_thirds": F.OrszagTwoThirds(), "three_halves": F.PaddedThreeHalves()}
+TOL = {64: 1e-12, 32: 1e-5}
+
+
+def rel(a, b):
+    return np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("deal", ["none", "two_thirds", "three_halves"])
+@pytest.mark.parametrize("N", [8, 12, 16, 24, 64, 96])
+def test_nonlinear_term_2d(N, deal, prec):
+    u, ks = solenoidal_2d(N, N)
+    got = F.compute_nonlinear_term(u, ks, dealiasing=DEAL[deal], spectral=F.GB300Spectral(prec))
+    ref = O.nonlinear_term(u, ks, deal)
+    assert rel(got, ref) < TOL[prec] * 10
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("deal", ["none", "two_thirds", "three_halves"])
+@pytest.mark.parametrize("N", [6, 8, 16, 20])
+def test_nonlinear_term_3d_non_hermitian(N, deal, prec):
+    u, ks = curl_noise_3d(N, 100 + N)      # complex-noise curl: NOT Hermitian (runtests.jl:509-515)
+    got = F.compute_nonlinear_term(u, ks, dealiasing=DEAL[deal], spectral=F.GB300Spectral(prec))
+    ref = O.nonlinear_term(u, ks, deal)
+    assert rel(got, ref) < TOL[prec] * 10
+
+
+def test_nonlinear_term_1d_and_direct_sum():
+    N = 8
+    x = np.arange(N) * 2 * np.pi / N
+    uh = (np.fft.fft(np.cos(x) + 0.3 * np.sin(2 * x)) / N)[:, None]
+    ks = F.wavenumber_grid((N,), (2 * np.pi,))
+    got = F.compute_nonlinear_term(uh, ks, dealiasing=F.NoDealiasing(), spectral=F.GB300Spectral(64))
+    assert np.allclose(got, nonlinear_term_direct(uh, ks, truncate=False), atol=1e-12)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_scalar_advection(prec):
+    u, ks = solenoidal_2d(12, 31)
+    th = scalar_2d(12, 32)
+    got = F.compute_nonlinear_term(th, ks, spectral=F.GB300Spectral(prec), advecting_hat=u)
+    assert rel(got, O.nonlinear_term(th, ks, "two_thirds", u)) < TOL[prec] * 10
+
+
+@pytest.mark.parametrize("ns,dims", [((64, 64), None), ((16, 16, 16), None), ((16, 16, 16), (1, 2)),
+                                     ((16, 16, 16), (3,)), ((12, 10), None)])
+def test_assign_shells_bit_identical(ns, dims):
+    ks = kgrid(ns)
+    geo = F.ShellMagnitude(dims)
+    for b, ob in [(F.LinearBinning(1.0), ("linear", 1.0)), (F.DyadicBinning(1.0), ("dyadic", 1.0)),
+                  (F.LinearBinning(0.7), ("linear", 0.7))]:
+        got = F.assign_shells_device(ks, b, geo)
+        _, _, _, ref = O.shell_setup(ks, ob, dims)
+        assert got.dtype == np.int64 and np.array_equal(got, ref)
+
+
+def test_spectral_flux_64sq_fp64_config1():
+    u, ks = spectrum_field((64, 64), e_config1, seed=1)
+    r = F.calculate_spectral_flux(u, ks, binning=F.LinearBinning(1.0), spectral=F.GB300Spectral(64))
+    c, T, P = O.spectral_flux(u, ks, ("linear", 1.0), "two_thirds")
+    assert len(r.transfer_spectrum) == 46
+    assert np.array_equal(r.k_shells, c)
+    assert rel(r.transfer_spectrum, T) < 1e-12
+    assert np.allclose(r.flux, np.cumsum(r.transfer_spectrum), atol=1e-14)
+
+
+@pytest.mark.parametrize("inv", ["ke", "enstrophy"])
+@pytest.mark.parametrize("deal", ["none", "two_thirds", "three_halves"])
+def test_spectral_flux_2d_invariants(inv, deal):
+    u, ks = solenoidal_2d(24, 5)
+    I = {"ke": F.KineticEnergy(), "enstrophy": F.Enstrophy()}[inv]
+    r = F.calculate_spectral_flux(u, ks, binning=F.LinearBinning(1.0), dealiasing=DEAL[deal], invariant=I,
+                                  spectral=F.GB300Spectral(64))
+    _, T, _ = O.spectral_flux(u, ks, ("linear", 1.0), deal, inv)
+    assert rel(r.transfer_spectrum, T) < 1e-11
+
+
+@pytest.mark.parametrize("inv", ["ke", "helicity", "enstrophy"])
+@pytest.mark.parametrize("dims", [None, (1, 2), (3,)])
+def test_spectral_flux_3d_non_hermitian(inv, dims):
+    u, ks = curl_noise_3d(12, 41)
+    I = {"ke": F.KineticEnergy(), "helicity": F.Helicity(), "enstrophy": F.Enstrophy()}[inv]
+    r = F.calculate_spectral_flux(u, ks, binning=F.LinearBinning(1.0), invariant=I, spectral=F.GB300Spectral(64),
+                                  geometry=F.ShellMagnitude(dims))
+    _, T, _ = O.spectral_flux(u, ks, ("linear", 1.0), "two_thirds", inv, dims=dims)
+    assert rel(r.transfer_spectrum, T) < 1e-11
+
+
+def test_scalar_flux_and_decomposed_flux():
+    u, ks = solenoidal_2d(16, 32)
+    th = scalar_2d(16, 33)
+    r = F.calculate_scalar_flux(u, th[..., 0], ks, binning=F.LinearBinning(1.0), spectral=F.GB300Spectral(64))
+    _, T, _ = O.spectral_flux(th, ks, ("linear", 1.0), "two_thirds", "scalar", adv_hat=u)
+    assert rel(r.transfer_spectrum, T) < 1e-11
+    u3, ks3 = curl_noise_3d(12, 51)
+    rh = F.calculate_spectral_flux(u3, ks3, binning=F.LinearBinning(1.0), decomposition=F.HelicalDecomposition(),
+                                   spectral=F.GB300Spectral(64))
+    comps = O.helical_decompose(u3, ks3)
+    for name in ("positive", "negative"):
+        _, T, _ = O.spectral_flux(u3, ks3, ("linear", 1.0), "two_thirds", carrier=comps[name])
+        assert rel(rh[name].transfer_spectrum, T) < 1e-11
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+@pytest.mark.parametrize("deal", ["none", "two_thirds", "three_halves"])
+def test_shell_to_shell_2d(prec, mode, deal):
+    u, ks = solenoidal_2d(16, 13)
+    r = F.calculate_shell_to_shell_transfer(u, ks, binning=F.LinearBinning(1.0), dealiasing=DEAL[deal],
+                                            spectral=F.GB300Spectral(prec), execution=F.GB300Execution(mode))
+    _, _, T, net, asym = O.shell_to_shell(u, ks, ("linear", 1.0), deal)
+    assert rel(r.transfer_matrix, T) < TOL[prec] * 10
+    assert rel(r.net_transfer, net) < TOL[prec] * 100
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("deal", ["two_thirds", "three_halves"])
+@pytest.mark.parametrize("inv", ["ke", "helicity"])
+def test_shell_to_shell_3d(prec, deal, inv):
+    u, ks = spectrum_field((16, 16, 16), e_config2, seed=3)
+    I = {"ke": F.KineticEnergy(), "helicity": F.Helicity()}[inv]
+    for mode in ("plain", "batched", "batched", "batched"):   # eager, capture, replay, replay
+        r = F.calculate_shell_to_shell_transfer(u, ks, binning=F.LinearBinning(2.0), dealiasing=DEAL[deal],
+                                                invariant=I, spectral=F.GB300Spectral(prec),
+                                                execution=F.GB300Execution(mode))
+        _, _, T, _, _ = O.shell_to_shell(u, ks, ("linear", 2.0), deal, inv)
+        assert rel(r.transfer_matrix, T) < TOL[prec] * 10, mode
+
+
+def test_scalar_shell_to_shell():
+    u, ks = solenoidal_2d(16, 14)
+    th = scalar_2d(16, 15)
+    r = F.calculate_scalar_shell_to_shell_transfer(u, th, ks, binning=F.LinearBinning(1.0),
+                                                   spectral=F.GB300Spectral(64))
+    _, _, T, _, _ = O.shell_to_shell(th, ks, ("linear", 1.0), "two_thirds", "scalar", adv_hat=u)
+    assert rel(r.transfer_matrix, T) < 1e-11
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_helical_partial_fluxes(prec):
+    u, ks = curl_noise_3d(12, 91)
+    for inv, oinv in ((F.KineticEnergy(), "ke"), (F.Helicity(), "helicity")):
+        r = F.calculate_partial_fluxes(u, ks, binning=F.LinearBinning(1.0), spectral=F.GB300Spectral(prec),
+                                       invariant=inv)
+        chans, _, _ = O.partial_fluxes(u, ks, "helical", ("linear", 1.0), "two_thirds", invariant=oinv)
+        scale = max(np.max(np.abs(c[0])) for c in chans.values())
+        for key, (T, _) in chans.items():
+            got = r.channels[key].transfer_spectrum
+            assert np.max(np.abs(got - T)) < TOL[prec] * 10 * scale, key
+
+
+def test_helmholtz_partial_fluxes():
+    u, ks = solenoidal_2d(16, 92)
+    r = F.calculate_partial_fluxes(u, ks, decomposition=F.HelmholtzDecomposition(), binning=F.LinearBinning(1.0),
+                                   spectral=F.GB300Spectral(64))
+    chans, _, _ = O.partial_fluxes(u, ks, "helmholtz", ("linear", 1.0), "two_thirds")
+    scale = max(np.max(np.abs(c[0])) for c in chans.values())
+    for key, (T, _) in chans.items():
+        assert np.max(np.abs(r.channels[key].transfer_spectrum - T)) < 1e-11 * scale
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+def test_mode_to_mode(fp64):
+    u, ks = solenoidal_2d(12, 21)
+    r = F.calculate_mode_to_mode_transfer(u, ks, spectral=F.GB300Spectral(64), fp64_products=fp64)
+    net, S = O.mode_to_mode_triad(u, ks, "two_thirds")
+    tol = 1e-12 if fp64 else 1e-5
+    assert rel(r.transfer, S) < tol * 10
+    assert rel(r.net_transfer, net) < tol * 100
+    u3, ks3 = curl_noise_3d(6, 7)
+    for inv, oi in ((F.KineticEnergy(), "ke"), (F.Helicity(), "helicity")):
+        r3 = F.calculate_mode_to_mode_transfer(u3, ks3, invariant=inv, force=True, fp64_products=fp64)
+        _, S3 = O.mode_to_mode_triad(u3, ks3, "two_thirds", oi)
+        assert rel(r3.transfer, S3) < tol * 10
+
+
+def test_transfer_density_and_decompositions():
+    u, ks = curl_noise_3d(8, 3)
+    Nh = O.nonlinear_term(u, ks, "two_thirds")
+    for inv, oi in ((F.KineticEnergy(), "ke"), (F.Helicity(), "helicity"), (F.Enstrophy(), "enstrophy")):
+        assert rel(F.transfer_density(inv, u, Nh, ks), O.transfer_density(oi, u, Nh, ks)) < 1e-12
+    d = F.decompose_field(F.HelicalDecomposition(), u, ks)
+    o = O.helical_decompose(u, ks)
+    assert rel(d["positive"], o["positive"]) < 1e-12 and rel(d["negative"], o["negative"]) < 1e-12
+    u2, ks2 = solenoidal_2d(8, 4)
+    h = F.decompose_field(F.HelmholtzDecomposition(), u2, ks2)
+    oh = O.helmholtz_decompose(u2, ks2)
+    assert rel(h["rotational"], oh["rotational"]) < 1e-12
+
+
+def test_errors_match_reference_behaviour():
+    u, ks = solenoidal_2d(8, 1)
+    with pytest.raises(ValueError):
+        F.calculate_spectral_flux(u, ks, invariant=F.Helicity())      # Helicity is 3D only
+    with pytest.raises(ValueError):
+        F.calculate_mode_to_mode_transfer(np.zeros((64, 64, 2), complex), kgrid((64, 64)))  # > max_modes
+    with pytest.raises(ValueError):
+        F.calculate_spectral_flux(u, ks, geometry=F.ParallelShells())   # dims=(3,) in 2D
+
+
+def test_zero_field_gives_zero():
+    ks = kgrid((6, 6))
+    r = F.calculate_shell_to_shell_transfer(np.zeros((6, 6, 2), complex), ks, binning=F.LinearBinning(1.0),
+                                            dealiasing=F.NoDealiasing(), verify_antisymmetry=False)
+    assert np.all(np.abs(r.transfer_matrix) < 1e-14) and np.isnan(r.max_antisymmetry_error)
