@@ -13,7 +13,7 @@ EXPORTS = [
     "fit_plan_create", "fit_plan_destroy", "fit_last_error", "fit_plan_set_stream", "fit_plan_info",
     "fit_launch_count", "fit_nonlinear_term", "fit_assign_shells", "fit_transfer_density",
     "fit_spectral_flux", "fit_shell_to_shell", "fit_helical_decompose", "fit_helmholtz_decompose",
-    "fit_partial_fluxes", "fit_mode_to_mode",
+    "fit_partial_fluxes", "fit_mode_to_mode", "fit_prof_enable", "fit_prof_read", "fit_prof_kind_name",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -47,8 +47,12 @@ def _declare(lib):
     lib.fit_helmholtz_decompose.argtypes = [vp, vp, vp, vp, i32]
     lib.fit_partial_fluxes.argtypes = [vp, vp, i32, i32, dp, i32, u32, i32, vp, i32]
     lib.fit_mode_to_mode.argtypes = [vp, vp, vp, i32, i32, vp, vp, i32]
+    lib.fit_prof_enable.argtypes = [i32]
+    lib.fit_prof_read.argtypes = [i32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    lib.fit_prof_kind_name.restype = C.c_char_p
+    lib.fit_prof_kind_name.argtypes = [i32]
     for name in EXPORTS:
-        if name not in ("fit_last_error", "fit_launch_count"):
+        if name not in ("fit_last_error", "fit_launch_count", "fit_prof_kind_name"):
             getattr(lib, name).restype = C.c_int
 
 
@@ -86,3 +90,19 @@ def check(rc: int):
 
 def launch_count() -> int:
     return int(load().fit_launch_count())
+
+
+def prof_enable(on: bool):
+    check(load().fit_prof_enable(int(on)))
+
+
+def prof_read_all():
+    """{kind name: (ms_total, algorithmic_bytes_total, launches)} since the last prof_enable."""
+    lib = load()
+    out = {}
+    for k in range(14):
+        ms, by, n = C.c_double(), C.c_double(), C.c_longlong()
+        check(lib.fit_prof_read(k, C.byref(ms), C.byref(by), C.byref(n)))
+        if n.value:
+            out[lib.fit_prof_kind_name(k).decode()] = (ms.value, by.value, n.value)
+    return out

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "fit_gb300.h"
@@ -15,6 +16,51 @@
 
 static thread_local char g_err[1024] = "";
 static std::atomic<long long> g_launches(0);
+
+// ---- per-launch profiling ------------------------------------------------------------------------
+struct ProfRec {
+  int kind;
+  double bytes;
+  cudaEvent_t a, b;
+};
+static std::mutex g_prof_mu;
+static std::vector<ProfRec> g_prof;
+static std::vector<cudaEvent_t> g_prof_pool;
+static size_t g_prof_used = 0;
+static bool g_prof_enabled = false;
+static const char* g_prof_names[PK_COUNT] = {"fft_strided", "fft_c2r_x", "fft_r2c_x", "gather", "product",
+                                             "bin", "carrier", "triad", "shell_table", "s2s_zinv", "s2s_yinv",
+                                             "s2s_xmix", "s2s_yfwd", "s2s_zfwd_bin"};
+
+static cudaEvent_t prof_event() {
+  if (g_prof_used < g_prof_pool.size()) return g_prof_pool[g_prof_used++];
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  g_prof_pool.push_back(e);
+  ++g_prof_used;
+  return e;
+}
+
+bool fit_prof_on() { return g_prof_enabled; }
+
+void fit_prof_begin(int kind, double bytes, cudaStream_t st) {
+  if (!g_prof_enabled) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  ProfRec r;
+  r.kind = kind;
+  r.bytes = bytes;
+  r.a = prof_event();
+  r.b = prof_event();
+  if (!r.a || !r.b) return;
+  cudaEventRecord(r.a, st);
+  g_prof.push_back(r);
+}
+
+void fit_prof_end(cudaStream_t st) {
+  if (!g_prof_enabled) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  if (!g_prof.empty()) cudaEventRecord(g_prof.back().b, st);
+}
 
 void fit_set_error(const char* fmt, ...) {
   va_list ap;
@@ -205,6 +251,36 @@ static int bin_into(fit_plan* p, const void* nh, long bstride, int nb, const voi
 extern "C" {
 
 const char* fit_last_error(void) { return fit_get_error(); }
+
+int fit_prof_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaDeviceSynchronize();
+  g_prof.clear();
+  g_prof_used = 0;
+  g_prof_enabled = on != 0;
+  return FIT_OK;
+}
+
+const char* fit_prof_kind_name(int kind) { return (kind >= 0 && kind < PK_COUNT) ? g_prof_names[kind] : ""; }
+
+int fit_prof_read(int kind, double* ms_total, double* bytes_total, long long* launches) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  FIT_CUDA_CHECK(cudaDeviceSynchronize());
+  double ms = 0.0, by = 0.0;
+  long long n = 0;
+  for (const ProfRec& r : g_prof) {
+    if (r.kind != kind) continue;
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) continue;
+    ms += t;
+    by += r.bytes;
+    ++n;
+  }
+  if (ms_total) *ms_total = ms;
+  if (bytes_total) *bytes_total = by;
+  if (launches) *launches = n;
+  return FIT_OK;
+}
 long long fit_launch_count(void) { return g_launches.load(); }
 
 int fit_plan_create(fit_plan** out, int nd, const int64_t* ns, int n_advected, int n_advecting, int dealias,

@@ -134,7 +134,9 @@ int gather_half(const GridDesc& g, const KTab& kt, const GatherArgs& a, typename
     return FIT_ERR_ARG;
   }
   dim3 grid(nblk(g.Mhalf, 256), a.nfields);
+  fit_prof_begin(PK_GATHER, (double)a.nfields * g.Mhalf * (sizeof(typename Vec2<T>::t) + 2.0 * (a.in_f64 ? 16 : 8)), st);
   k_gather<typename Vec2<T>::t><<<grid, 256, 0, st>>>(g, kt, a, out);
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -157,7 +159,9 @@ __global__ void k_product(const T* __restrict__ u, const T* __restrict__ grad, T
 
 template <typename T>
 int product(const T* u, const T* grad, T* out, int nd, int M, long n, cudaStream_t st) {
+  fit_prof_begin(PK_PRODUCT, (double)(nd + M * nd + M) * n * sizeof(T), st);
   k_product<T><<<nblk(n, 256), 256, 0, st>>>(u, grad, out, nd, M, n);
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -241,8 +245,10 @@ int effective_carrier(const GridDesc& g, const KTab& kt, const void* carrier, in
     fit_set_error("effective carrier supports at most 3 components");
     return FIT_ERR_ARG;
   }
+  fit_prof_begin(PK_CARRIER, (double)g.Mhalf * nceff * (sizeof(typename Vec2<T>::t) + 2.0 * (in_f64 ? 16 : 8)), st);
   k_ceff<typename Vec2<T>::t><<<nblk(g.Mhalf, 256), 256, 0, st>>>(g, kt, carrier, in_f64, comp_stride, ncomp_carrier,
                                                                  invariant, two_thirds, shell_full, ceff, nceff, seff);
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -322,8 +328,10 @@ int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_
       return FIT_ERR_CUDA;
     }
   }
+  fit_prof_begin(PK_BIN, (double)g.Mhalf * ((nb + 1) * nc * sizeof(typename Vec2<T>::t) + 2.0), st);
   k_bin<typename Vec2<T>::t><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, nc, seff, g.Mhalf, nsh,
                                                         partial);
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   k_reduce_partials<<<nblk(nbins, 128), 128, 0, st>>>(partial, nblocks, nbins, out);
   FIT_LAUNCH_CHECK();

@@ -149,6 +149,7 @@ int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const 
     return FIT_ERR_SIZE;
   }
   const V* tw = axis_tw<T>(ax);
+  fit_prof_begin(PK_FFT_STRIDED, 2.0 * (double)P * ax.N * Q * sizeof(V), st);
 #define FIT_PS_LAUNCH(INV, EPT)                                                                          \
   do {                                                                                                 \
     FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, t.smem));                                         \
@@ -161,6 +162,7 @@ int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const 
     if (t.EPT == 8) FIT_PS_LAUNCH(false, 8); else FIT_PS_LAUNCH(false, 16);
   }
 #undef FIT_PS_LAUNCH
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -172,6 +174,7 @@ int pass_c2r_x(const typename Vec2<T>::t* in, T* out, const Axis& ax, long L, T 
   Tile t = pick_tile(ax.N, sizeof(V), (L + 1) / 2);
   const long grid = (L + 2L * t.C - 1) / (2L * t.C);
   const V* tw = axis_tw<T>(ax);
+  fit_prof_begin(PK_FFT_C2R_X, (double)L * ((ax.N / 2 + 1) * sizeof(V) + ax.N * sizeof(T)), st);
   if (t.EPT == 8) {
     FIT_TRY(prep_kernel(k_c2r_x<V, 8>, t.smem));
     k_c2r_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
@@ -179,6 +182,7 @@ int pass_c2r_x(const typename Vec2<T>::t* in, T* out, const Axis& ax, long L, T 
     FIT_TRY(prep_kernel(k_c2r_x<V, 16>, t.smem));
     k_c2r_x<V, 16><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
   }
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -190,6 +194,7 @@ int pass_r2c_x(const T* in, typename Vec2<T>::t* out, const Axis& ax, long L, T 
   Tile t = pick_tile(ax.N, sizeof(V), (L + 1) / 2);
   const long grid = (L + 2L * t.C - 1) / (2L * t.C);
   const V* tw = axis_tw<T>(ax);
+  fit_prof_begin(PK_FFT_R2C_X, (double)L * ((ax.N / 2 + 1) * sizeof(V) + ax.N * sizeof(T)), st);
   if (t.EPT == 8) {
     FIT_TRY(prep_kernel(k_r2c_x<V, 8>, t.smem));
     k_r2c_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
@@ -197,6 +202,7 @@ int pass_r2c_x(const T* in, typename Vec2<T>::t* out, const Axis& ax, long L, T 
     FIT_TRY(prep_kernel(k_r2c_x<V, 16>, t.smem));
     k_r2c_x<V, 16><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
   }
+  fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }

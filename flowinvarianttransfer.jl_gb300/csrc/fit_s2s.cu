@@ -171,6 +171,9 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
     s->key_gen = p->buf_gen;
     return FIT_OK;
   }
+  if (fit_prof_on()) {   // per-launch events need eager launches
+    return (p->prec == 64) ? run_batched<double>(p, s, ud, ad, inv, Td) : run_batched<float>(p, s, ud, ad, inv, Td);
+  }
   if (s->exec) {
     FIT_CUDA_CHECK(cudaGraphLaunch(s->exec, p->stream));
     fit_count_launches(s->graph_launches);

@@ -220,9 +220,11 @@ static int triad_run(fit_plan* p, const void* u, const void* adv, int inv, doubl
   k_triad_prep<V><<<nb, 256, 0, p->stream>>>(p->g, p->kt, t, u, adv, p->io_f64, M, inv, A, F, C);
   FIT_LAUNCH_CHECK();
   dim3 grid(nb, nchunk);
+  fit_prof_begin(PK_TRIAD, 8.0 * (double)t.Nm * (double)t.Nm, p->stream);
   if (M == 1) launch_triad<V, 1>(grid, t, p->kt, A, F, C, pch, S, part, p->stream);
   else if (M == 2) launch_triad<V, 2>(grid, t, p->kt, A, F, C, pch, S, part, p->stream);
   else launch_triad<V, 3>(grid, t, p->kt, A, F, C, pch, S, part, p->stream);
+  fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   k_triad_net<<<nb, 256, 0, p->stream>>>(part, nchunk, t.Nm, net);
   FIT_LAUNCH_CHECK();

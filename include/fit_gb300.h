@@ -71,6 +71,12 @@ int fit_plan_set_stream(fit_plan* plan, void* stream);
 int fit_plan_info(const fit_plan* plan, int64_t* info, int n);
 /* Number of library kernels launched since load (graph replays count their kernels). */
 long long fit_launch_count(void);
+/* Per-launch profiling: when enabled, every launch is bracketed by CUDA events and tagged with its
+ * algorithmic DRAM bytes (captured graphs are bypassed while enabled). fit_prof_read sums one
+ * kernel kind (0..13, named by fit_prof_kind_name) since the last fit_prof_enable. */
+int fit_prof_enable(int on);
+int fit_prof_read(int kind, double* ms_total, double* bytes_total, long long* launches);
+const char* fit_prof_kind_name(int kind);
 
 /* N̂ = FFT[(u_adv·∇) f] in the reference normalisation. Replaces
  * NonlinearTerm._compute_nonlinear_term! (src/NonlinearTerm.jl:102-116) for the FFT backend:

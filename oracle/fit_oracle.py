@@ -22,13 +22,37 @@ import math
 
 import numpy as np
 
+_WORKERS = None
+
+
+def set_fft_workers(n):
+    """Use scipy.fft with ``n`` threads for every transform (the reference uses FFTW threads /
+    OhMyThreads for the same transforms); ``None`` restores single-threaded numpy.fft."""
+    global _WORKERS
+    _WORKERS = n
+
+
+def _fftn(a, axes):
+    if _WORKERS:
+        import scipy.fft as sf
+        return sf.fftn(a, axes=axes, workers=_WORKERS)
+    return np.fft.fftn(a, axes=axes)
+
+
+def _ifftn(a, axes):
+    if _WORKERS:
+        import scipy.fft as sf
+        return sf.ifftn(a, axes=axes, workers=_WORKERS)
+    return np.fft.ifftn(a, axes=axes)
+
+
 __all__ = [
     "wavenumber_grid", "keep_mask", "shell_coordinate", "julia_range", "shell_edges",
     "shell_centers", "assign_shells", "padded_len", "embed_spectrum", "truncate_spectrum",
     "nonlinear_term", "dealias_copy", "transfer_density", "spectral_flux", "shell_to_shell",
     "helical_decompose", "toroidal_poloidal_decompose", "helmholtz_decompose", "partial_fluxes",
     "mode_to_mode", "mode_to_mode_triad", "default_binning", "filter_response",
-    "coarse_graining_flux", "shell_setup",
+    "coarse_graining_flux", "shell_setup", "set_fft_workers", "s2s_setup", "s2s_column",
 ]
 
 
@@ -238,24 +262,24 @@ def nonlinear_term(f_hat, ks, dealiasing="two_thirds", adv_hat=None):
     if dealiasing == "three_halves":
         Ms = tuple(padded_len(n) for n in ns)
         scale = float(np.prod(Ms)) / Np ** 2
-        uM = [np.real(np.fft.ifftn(embed_spectrum(adv[..., j], Ms), axes=axes)) for j in range(nd)]
+        uM = [np.real(_ifftn(embed_spectrum(adv[..., j], Ms), axes=axes)) for j in range(nd)]
         for c in range(M):
             NcM = np.zeros(Ms)
             for j in range(nd):
-                gMj = np.real(np.fft.ifftn(embed_spectrum(1j * kc[j] * f_hat[..., c], Ms), axes=axes))
+                gMj = np.real(_ifftn(embed_spectrum(1j * kc[j] * f_hat[..., c], Ms), axes=axes))
                 NcM = NcM + uM[j] * gMj
-            out[..., c] = truncate_spectrum(np.fft.fftn(NcM, axes=axes), ns) * scale
+            out[..., c] = truncate_spectrum(_fftn(NcM, axes=axes), ns) * scale
         return out
     trunc = dealiasing == "two_thirds"
     if dealiasing not in ("two_thirds", "none"):
         raise ValueError(f"unknown dealiasing {dealiasing!r}")
     keep = keep_mask(ns) if trunc else np.ones(ns, dtype=bool)
-    u = [np.real(np.fft.ifftn(keep * adv[..., j], axes=axes)) for j in range(nd)]
+    u = [np.real(_ifftn(keep * adv[..., j], axes=axes)) for j in range(nd)]
     for c in range(M):
         Nc = np.zeros(ns)
         for j in range(nd):
-            Nc = Nc + u[j] * np.real(np.fft.ifftn(1j * kc[j] * keep * f_hat[..., c], axes=axes))
-        Nh = np.fft.fftn(Nc, axes=axes) / Np
+            Nc = Nc + u[j] * np.real(_ifftn(1j * kc[j] * keep * f_hat[..., c], axes=axes))
+        Nh = _fftn(Nc, axes=axes) / Np
         out[..., c] = Nh * keep if trunc else Nh
     return out
 
@@ -403,6 +427,50 @@ def spectral_flux(u_hat, ks, binning=None, dealiasing="two_thirds", invariant="k
     return centers, T, np.cumsum(T)
 
 
+def s2s_setup(u_hat, ks, binning=None, dealiasing="two_thirds", invariant="ke", adv_hat=None, dims=None):
+    """Mediator-independent part of ``_shell_to_shell_fft!``
+    (``ext/FlowInvariantTransferFFTWExt.jl:209-237``): shells, truncated copies and the advecting
+    velocity in physical space (computed once)."""
+    binning = default_binning(ks) if binning is None else binning
+    nd = len(ks)
+    ns = u_hat.shape[:nd]
+    adv = u_hat if adv_hat is None else adv_hat
+    _, edges, centers, sidx = shell_setup(ks, binning, dims)
+    trunc = dealiasing == "two_thirds"
+    keep = keep_mask(ns)
+    st = dict(u_hat=u_hat, ks=ks, nd=nd, ns=ns, M=u_hat.shape[nd], adv=adv, edges=edges, centers=centers,
+              sidx=sidx, nsh=len(centers), Np=float(np.prod(ns)), trunc=trunc,
+              padded=dealiasing == "three_halves", keep=keep, invariant=invariant,
+              axes=tuple(range(nd)), kc=[_kcomp(ks, d, ns) for d in range(nd)])
+    st["vhat"] = u_hat * keep[..., None] if trunc else u_hat
+    if not st["padded"]:
+        ahat = adv * keep[..., None] if trunc else adv
+        st["u_full"] = [np.real(_ifftn(ahat[..., j], axes=st["axes"])) for j in range(nd)]
+    return st
+
+
+def s2s_column(st, m, comps=None):
+    """Column m (0-based) of T: ``ext/FlowInvariantTransferFFTWExt.jl:245-275``. ``comps``
+    restricts the advected components evaluated (a bounded CPU timing sample); the column is
+    then the partial sum over those components."""
+    nd, ns, M, axes, kc = st["nd"], st["ns"], st["M"], st["axes"], st["kc"]
+    um = st["vhat"] * (st["sidx"] == m + 1)[..., None]
+    comps = range(M) if comps is None else comps
+    if st["padded"]:
+        Nh = nonlinear_term(um, st["ks"], "three_halves", st["adv"])
+    else:
+        Nh = np.zeros(ns + (M,), dtype=np.complex128)
+        for c in comps:
+            Nc = np.zeros(ns)
+            for j in range(nd):
+                Nc = Nc + st["u_full"][j] * np.real(_ifftn(1j * kc[j] * um[..., c], axes=axes))
+            Nh[..., c] = _fftn(Nc, axes=axes) / st["Np"]
+        if st["trunc"]:
+            Nh = Nh * st["keep"][..., None]
+    t = transfer_density(st["invariant"], st["u_hat"], Nh, st["ks"])
+    return _bin(t, st["sidx"], st["nsh"])
+
+
 def shell_to_shell(u_hat, ks, binning=None, dealiasing="two_thirds", invariant="ke",
                    adv_hat=None, dims=None, verify=True, mediators=None):
     """(centers, edges, T[n,m], net, max_asym). Restates ``_shell_to_shell_fft!``
@@ -410,43 +478,15 @@ def shell_to_shell(u_hat, ks, binning=None, dealiasing="two_thirds", invariant="
     advects the band-m field taken from the truncated copy; the carrier is the untruncated
     field; no antisymmetrisation. ``mediators`` (0-based) limits the columns computed (for a
     bounded CPU timing sample); the others stay zero."""
-    binning = default_binning(ks) if binning is None else binning
-    nd = len(ks)
-    ns = u_hat.shape[:nd]
-    M = u_hat.shape[nd]
-    adv = u_hat if adv_hat is None else adv_hat
-    _, edges, centers, sidx = shell_setup(ks, binning, dims)
-    nsh = len(centers)
-    Np = float(np.prod(ns))
-    trunc = dealiasing == "two_thirds"
-    padded = dealiasing == "three_halves"
-    keep = keep_mask(ns)
-    vhat = u_hat * keep[..., None] if trunc else u_hat
-    axes = tuple(range(nd))
-    kc = [_kcomp(ks, d, ns) for d in range(nd)]
-    if not padded:
-        ahat = adv * keep[..., None] if trunc else adv
-        u_full = [np.real(np.fft.ifftn(ahat[..., j], axes=axes)) for j in range(nd)]
+    st = s2s_setup(u_hat, ks, binning, dealiasing, invariant, adv_hat, dims)
+    nsh = st["nsh"]
     T = np.zeros((nsh, nsh))
     cols = range(nsh) if mediators is None else mediators
     for m in cols:
-        um = vhat * (sidx == m + 1)[..., None]
-        if padded:
-            Nh = nonlinear_term(um, ks, "three_halves", adv)
-        else:
-            Nh = np.zeros(ns + (M,), dtype=np.complex128)
-            for c in range(M):
-                Nc = np.zeros(ns)
-                for j in range(nd):
-                    Nc = Nc + u_full[j] * np.real(np.fft.ifftn(1j * kc[j] * um[..., c], axes=axes))
-                Nh[..., c] = np.fft.fftn(Nc, axes=axes) / Np
-            if trunc:
-                Nh = Nh * keep[..., None]
-        t = transfer_density(invariant, u_hat, Nh, ks)
-        T[:, m] = _bin(t, sidx, nsh)
+        T[:, m] = s2s_column(st, m)
     net = T.sum(axis=1)
     asym = float(np.max(np.abs(T + T.T))) if verify else float("nan")
-    return centers, edges, T, net, asym
+    return st["centers"], st["edges"], T, net, asym
 
 
 def partial_fluxes(u_hat, ks, decomposition="helical", binning=None, dealiasing="two_thirds",
@@ -602,11 +642,11 @@ def coarse_graining_flux(u_phys, ks, ell, kind="gaussian"):
     G = filter_response(kind, kmag, ell)
 
     def filt(f):
-        return np.real(np.fft.ifftn(G * np.fft.fftn(f, axes=axes), axes=axes))
+        return np.real(_ifftn(G * _fftn(f, axes=axes), axes=axes))
 
     ub = [filt(u_phys[..., i]) for i in range(nd)]
-    ubh = [np.fft.fftn(ub[i], axes=axes) for i in range(nd)]
-    grad = [[np.real(np.fft.ifftn(1j * kc[j] * ubh[i], axes=axes)) for j in range(nd)] for i in range(nd)]
+    ubh = [_fftn(ub[i], axes=axes) for i in range(nd)]
+    grad = [[np.real(_ifftn(1j * kc[j] * ubh[i], axes=axes)) for j in range(nd)] for i in range(nd)]
     Pi = np.zeros(ns)
     for i in range(nd):
         for j in range(nd):
