@@ -237,3 +237,50 @@ int triad_m2m(fit_plan* p, const void* u, const void* adv, int inv, int fp64, do
 }
 
 }  // namespace fit
+
+namespace fit {
+
+// Same three launches as triad_run, with the A/F/C tables and the per-chunk net partials placed
+// in caller-provided scratch (used by the allocation-free entry point in fit_noalloc.cu).
+int triad_run_scratch(const GridDesc& g, const KTab& kt, int M, int two_thirds, int io_f64, const void* u,
+                      const void* adv, int inv, int fp64, void* scratch, int nchunk, double* S, double* net,
+                      cudaStream_t st) {
+  TriadArgs t;
+  t.nd = g.nd;
+  for (int d = 0; d < 3; ++d) t.N[d] = g.N[d];
+  t.Nm = g.Ntot;
+  t.two_thirds = two_thirds;
+  t.norm = 0.5 / ((double)t.Nm * (double)t.Nm);
+  const long pch = (t.Nm + nchunk - 1) / nchunk;
+  const unsigned nb = (unsigned)((t.Nm + 255) / 256);
+  dim3 grid(nb, nchunk);
+  if (fp64) {
+    double2* A = (double2*)scratch;
+    double2* F = A + t.Nm * t.nd;
+    double2* C = F + t.Nm * M;
+    double* part = (double*)(C + t.Nm * M);
+    k_triad_prep<double2><<<nb, 256, 0, st>>>(g, kt, t, u, adv, io_f64, M, inv, A, F, C);
+    FIT_LAUNCH_CHECK();
+    if (M == 1) launch_triad<double2, 1>(grid, t, kt, A, F, C, pch, S, part, st);
+    else if (M == 2) launch_triad<double2, 2>(grid, t, kt, A, F, C, pch, S, part, st);
+    else launch_triad<double2, 3>(grid, t, kt, A, F, C, pch, S, part, st);
+    FIT_LAUNCH_CHECK();
+    k_triad_net<<<nb, 256, 0, st>>>(part, nchunk, t.Nm, net);
+  } else {
+    float2* A = (float2*)scratch;
+    float2* F = A + t.Nm * t.nd;
+    float2* C = F + t.Nm * M;
+    double* part = (double*)(C + t.Nm * M);
+    k_triad_prep<float2><<<nb, 256, 0, st>>>(g, kt, t, u, adv, io_f64, M, inv, A, F, C);
+    FIT_LAUNCH_CHECK();
+    if (M == 1) launch_triad<float2, 1>(grid, t, kt, A, F, C, pch, S, part, st);
+    else if (M == 2) launch_triad<float2, 2>(grid, t, kt, A, F, C, pch, S, part, st);
+    else launch_triad<float2, 3>(grid, t, kt, A, F, C, pch, S, part, st);
+    FIT_LAUNCH_CHECK();
+    k_triad_net<<<nb, 256, 0, st>>>(part, nchunk, t.Nm, net);
+  }
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+}  // namespace fit

@@ -131,6 +131,19 @@ int fit_partial_fluxes(fit_plan* plan, const void* u_hat, int decomposition, int
 int fit_mode_to_mode(fit_plan* plan, const void* u_hat, const void* adv_hat, int invariant, int fp64_products,
                      double* S, double* net, int ptr_kind);
 
+/* Allocation-free variant of fit_mode_to_mode, for callers that cannot allocate device memory
+ * (a caller-owned memory budget or allocator, a latency-critical loop where an allocation would
+ * synchronise the device, an embedding runtime that only lends its own buffers). It has no
+ * counterpart in the reference. Every array argument is a device pointer (ks_dev: nd device
+ * arrays); no plan is used and nothing is allocated: intermediates live in one fixed 6.5 MiB
+ * device array that each GPU loading the library holds until exit. Grids of at most 32768 modes
+ * (32^3); larger grids return FIT_ERR_SIZE. The first call on a device looks up that array's
+ * device address (do it before any stream capture). Calls share the array, so calls that
+ * overlap on the GPU race: serialise them per device. stream may be NULL (default stream). */
+int fit_mode_to_mode_noalloc(int nd, const int64_t* ns, int n_advected, int n_advecting, int dealias,
+                             const double* const* ks_dev, int invariant, int fp64_products, int io_f64,
+                             const void* u_hat, const void* adv_hat, double* S, double* net, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
