@@ -288,3 +288,212 @@ __global__ void __launch_bounds__(1024) k_r2c_x(const typename Scal<V>::t* __res
 }
 
 }  // namespace fit
+
+// =============================================================================================
+// Compile-time engine: transform length, radix schedule, tile width and thread count are all
+// template constants, so every index computation folds to shifts / constant multiplies and
+// every stage is fully unrolled (no runtime radix dispatch, no local-memory spills).
+// =============================================================================================
+namespace fit {
+
+__host__ __device__ constexpr int ct_p2(int n) { int p = 0; while (n % 2 == 0) { n /= 2; ++p; } return p; }
+__host__ __device__ constexpr int ct_odd(int n) { while (n % 2 == 0) n /= 2; return n; }
+__host__ __device__ constexpr int ct_nst(int N) {
+  int p2 = ct_p2(N), n = ct_odd(N), c = p2 / 3 + (p2 % 3 != 0 ? 1 : 0);
+  while (n % 3 == 0) { n /= 3; ++c; }
+  while (n % 5 == 0) { n /= 5; ++c; }
+  return c;
+}
+__host__ __device__ constexpr int ct_radix(int N, int s) {
+  const int p2 = ct_p2(N), n8 = p2 / 3, rem = p2 % 3;
+  if (s < n8) return 8;
+  int idx = n8;
+  if (rem) {
+    if (s == idx) return rem == 2 ? 4 : 2;
+    ++idx;
+  }
+  int n = ct_odd(N), n3 = 0;
+  while (n % 3 == 0) { n /= 3; ++n3; }
+  if (s < idx + n3) return 3;
+  return 5;
+}
+__host__ __device__ constexpr int ct_span(int N, int s) { int p = 1; for (int i = 0; i < s; ++i) p *= ct_radix(N, i); return p; }
+__host__ __device__ constexpr int ct_pow2floor(int x) { int p = 1; while (p * 2 <= x) p *= 2; return p; }
+
+template <typename V, int N>
+struct CtTile {
+  static constexpr int VB = (int)sizeof(V);
+  static constexpr int Cmin = 128 / VB;
+  static constexpr int Cw = ct_pow2floor((VB == 8 ? 4096 : 2048) / N > 0 ? (VB == 8 ? 4096 : 2048) / N : 1);
+  static constexpr int C = Cw > Cmin ? Cw : Cmin;
+  static constexpr int E = C * N;
+  static constexpr int EPT = E <= 8192 ? 8 : 16;
+  static constexpr int NTHR = (E / EPT + 31) / 32 * 32;
+  static constexpr size_t SMEM = (size_t)(E + N) * VB;
+};
+
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS>
+__device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
+  constexpr int MAXB = (EPT + R - 1) / R;
+  constexpr int NR = N / R;
+  constexpr int NB = C * NR;
+  constexpr int TS = N / (NS * R);
+  V v[MAXB][R];
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = tid + i * NTHR;
+    if (NB % NTHR == 0 || b < NB) {
+      const int c = b % C;
+      const int j = b / C;
+      const int k = j % NS;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        V x = s[swz(j + q * NR, c, C)];
+        if (NS > 1 && q > 0) {
+          V w = tw[k * q * TS];
+          if (INV) w.y = -w.y;
+          x = cmul(x, w);
+        }
+        v[i][q] = x;
+      }
+      dftr<V, R, INV>(v[i]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = tid + i * NTHR;
+    if (NB % NTHR == 0 || b < NB) {
+      const int c = b % C;
+      const int j = b / C;
+      const int k = j % NS;
+      const int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) s[swz(base + q * NS, c, C)] = v[i][q];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S>
+__device__ __forceinline__ void ct_stages(V* s, const V* tw, int tid) {
+  if constexpr (S < ct_nst(N)) {
+    ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S)>(s, tw, tid);
+    ct_stages<V, INV, N, C, NTHR, EPT, S + 1>(s, tw, tid);
+  }
+}
+
+template <typename V, bool INV, int N>
+__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_strided(const V* in, V* out, long P, long tilesPerQ,
+                                                                  const V* __restrict__ twg,
+                                                                  typename Scal<V>::t scale) {
+  typedef CtTile<V, N> TT;
+  constexpr int C = TT::C, E = TT::E;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + E;
+  const int tid = threadIdx.x;
+  const long tile = blockIdx.x;
+  const long q = tile / tilesPerQ;
+  const long c0 = (tile - q * tilesPerQ) * C;
+  const long base = q * P * (long)N;
+  for (int t = tid; t < N; t += TT::NTHR) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i % C, e = i / C;
+    const long col = c0 + c;
+    V x = mkc<V>(0, 0);
+    if (col < P) x = in[base + col + (long)e * P];
+    s[swz(e, c, C)] = x;
+  }
+  __syncthreads();
+  ct_stages<V, INV, N, C, TT::NTHR, TT::EPT, 0>(s, tw, tid);
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i % C, e = i / C;
+    const long col = c0 + c;
+    if (col < P) out[base + col + (long)e * P] = cscale(s[swz(e, c, C)], scale);
+  }
+}
+
+template <typename V, int N>
+__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_c2r_x(const V* __restrict__ in,
+                                                                typename Scal<V>::t* __restrict__ out, long L,
+                                                                const V* __restrict__ twg,
+                                                                typename Scal<V>::t scale) {
+  typedef CtTile<V, N> TT;
+  constexpr int C = TT::C, E = TT::E, Nh = N / 2 + 1;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + E;
+  const int tid = threadIdx.x;
+  const long l0 = (long)blockIdx.x * 2 * C;
+  for (int t = tid; t < N; t += TT::NTHR) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i / N, k = i % N;
+    const long a = l0 + 2 * c, b = a + 1;
+    const bool cj = 2 * k > N;
+    const int kk = cj ? N - k : k;
+    const bool selfc = (k == 0) || (2 * k == N);
+    V A = mkc<V>(0, 0), B = mkc<V>(0, 0);
+    if (a < L) {
+      A = in[a * Nh + kk];
+      if (cj) A.y = -A.y;
+      if (selfc) A.y = 0;
+    }
+    if (b < L) {
+      B = in[b * Nh + kk];
+      if (cj) B.y = -B.y;
+      if (selfc) B.y = 0;
+    }
+    s[swz(k, c, C)] = mkc<V>(A.x - B.y, A.y + B.x);
+  }
+  __syncthreads();
+  ct_stages<V, true, N, C, TT::NTHR, TT::EPT, 0>(s, tw, tid);
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i / N, x = i % N;
+    const long a = l0 + 2 * c, b = a + 1;
+    const V z = s[swz(x, c, C)];
+    if (a < L) out[a * N + x] = z.x * scale;
+    if (b < L) out[b * N + x] = z.y * scale;
+  }
+}
+
+template <typename V, int N>
+__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_r2c_x(const typename Scal<V>::t* __restrict__ in,
+                                                                V* __restrict__ out, long L,
+                                                                const V* __restrict__ twg,
+                                                                typename Scal<V>::t scale) {
+  typedef CtTile<V, N> TT;
+  typedef typename Scal<V>::t S;
+  constexpr int C = TT::C, E = TT::E, Nh = N / 2 + 1;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + E;
+  const int tid = threadIdx.x;
+  const long l0 = (long)blockIdx.x * 2 * C;
+  for (int t = tid; t < N; t += TT::NTHR) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i / N, x = i % N;
+    const long a = l0 + 2 * c, b = a + 1;
+    const S ra = (a < L) ? in[a * N + x] : (S)0;
+    const S rb = (b < L) ? in[b * N + x] : (S)0;
+    s[swz(x, c, C)] = mkc<V>(ra, rb);
+  }
+  __syncthreads();
+  ct_stages<V, false, N, C, TT::NTHR, TT::EPT, 0>(s, tw, tid);
+  const S hs = (S)0.5 * scale;
+  for (int i = tid; i < C * Nh; i += TT::NTHR) {
+    const int c = i / Nh, k = i % Nh;
+    const long a = l0 + 2 * c, b = a + 1;
+    const V zk = s[swz(k, c, C)];
+    const V zn = s[swz(k == 0 ? 0 : N - k, c, C)];
+    if (a < L) out[a * Nh + k] = mkc<V>((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+    if (b < L) out[b * Nh + k] = mkc<V>((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+  }
+}
+
+}  // namespace fit

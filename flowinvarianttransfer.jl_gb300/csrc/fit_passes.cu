@@ -10,6 +10,16 @@
 
 namespace fit {
 
+template <typename T>
+int ct_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, int N, long P, long Q, bool inv, T scale,
+               const typename Vec2<T>::t* tw, cudaStream_t st);
+template <typename T>
+int ct_c2r(const typename Vec2<T>::t* in, T* out, int N, long L, T scale, const typename Vec2<T>::t* tw,
+           cudaStream_t st);
+template <typename T>
+int ct_r2c(const T* in, typename Vec2<T>::t* out, int N, long L, T scale, const typename Vec2<T>::t* tw,
+           cudaStream_t st);
+
 int axis_init(Axis* a, int N) {
   a->N = N;
   a->tw32 = nullptr;
@@ -150,6 +160,15 @@ int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const 
   }
   const V* tw = axis_tw<T>(ax);
   fit_prof_begin(PK_FFT_STRIDED, 2.0 * (double)P * ax.N * Q * sizeof(V), st);
+  {
+    const int rc = ct_strided<T>(in, out, ax.N, P, Q, inverse, scale, tw, st);
+    if (rc != 1) {
+      fit_prof_end(st);
+      if (rc != FIT_OK) return rc;
+      FIT_LAUNCH_CHECK();
+      return FIT_OK;
+    }
+  }
 #define FIT_PS_LAUNCH(INV, EPT)                                                                          \
   do {                                                                                                 \
     FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, t.smem));                                         \
@@ -175,6 +194,15 @@ int pass_c2r_x(const typename Vec2<T>::t* in, T* out, const Axis& ax, long L, T 
   const long grid = (L + 2L * t.C - 1) / (2L * t.C);
   const V* tw = axis_tw<T>(ax);
   fit_prof_begin(PK_FFT_C2R_X, (double)L * ((ax.N / 2 + 1) * sizeof(V) + ax.N * sizeof(T)), st);
+  {
+    const int rc = ct_c2r<T>(in, out, ax.N, L, scale, tw, st);
+    if (rc != 1) {
+      fit_prof_end(st);
+      if (rc != FIT_OK) return rc;
+      FIT_LAUNCH_CHECK();
+      return FIT_OK;
+    }
+  }
   if (t.EPT == 8) {
     FIT_TRY(prep_kernel(k_c2r_x<V, 8>, t.smem));
     k_c2r_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
@@ -195,6 +223,15 @@ int pass_r2c_x(const T* in, typename Vec2<T>::t* out, const Axis& ax, long L, T 
   const long grid = (L + 2L * t.C - 1) / (2L * t.C);
   const V* tw = axis_tw<T>(ax);
   fit_prof_begin(PK_FFT_R2C_X, (double)L * ((ax.N / 2 + 1) * sizeof(V) + ax.N * sizeof(T)), st);
+  {
+    const int rc = ct_r2c<T>(in, out, ax.N, L, scale, tw, st);
+    if (rc != 1) {
+      fit_prof_end(st);
+      if (rc != FIT_OK) return rc;
+      FIT_LAUNCH_CHECK();
+      return FIT_OK;
+    }
+  }
   if (t.EPT == 8) {
     FIT_TRY(prep_kernel(k_r2c_x<V, 8>, t.smem));
     k_r2c_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
