@@ -1,0 +1,365 @@
+// Fused FP32 shell-to-shell pipeline for cubic 3D grids (2/3 or 3/2 dealiasing).
+//
+// Every mediator m needs N_m = (u . grad) u_m, u_m = u restricted to shell m, and then
+// T(n, m) = sum over shell n of Re(conj(C) N_m). Only the "live box" of the spectrum can be
+// non-zero: |k_d| <= K with K = N div 3 - 1 (2/3 rule) or K = floor(N/2) (data grid embedded in
+// the 3/2 padded grid). The pipeline keeps every spectral intermediate restricted to that box
+// (kx in [0, K], ky/kz in [-K, K], stored compactly with index f + K), fuses the derivative
+// multipliers, masks and scalings into the transform passes, computes the physical-space
+// product inside the x pass (inverse x transform -> product with the advecting velocity ->
+// forward x transform in one kernel), and bins the transfer density inside the last forward
+// pass (no N_m field is written):
+//
+//   zinv  : z pass of H * [shell == m] and of ik_z * H * [shell == m]        (6 outputs / m)
+//   yinv  : y pass -> Y(P), Y(ik_y P), Y(Q)   (P, Q = the two zinv outputs)   (9 outputs / m)
+//   xmix  : per component c: sum_j u_j * C2R(ik_x? G_cj) -> R2C -> kx <= K     (3 outputs / m)
+//   yfwd  : y pass forward, keep ky in [-K, K]                                 (3 outputs / m)
+//   zfwd  : z pass forward, t = sum_c Re(conj(Ceff_c) N_c), FP64 shell bins per block
+//
+// Layouts (complex64 unless noted): live pencils col = kx + KX*ky' (P1 = KX*KY of them);
+//   H, Ceff   [c][kz'][col]           seff, sb (uint16) [kz'][col]
+//   zinv out  [b][c][v][z][col]        yinv out [b][c][j][z][y][kx]
+//   xmix out  [b][c][line = y + N z][kx]   yfwd out [b][c][z][ky'][kx]
+#pragma once
+
+#include "fit_fft.cuh"
+#include "fit_maps.cuh"
+
+namespace fit {
+
+struct FzArgs {
+  int K, KX, KY;
+  long P1;      // KX * KY live pencils
+  long L;       // N * N lines of the x pass
+  int nsh;
+  int nb;       // mediators in this launch
+  int med[16];  // their shell numbers (1-based)
+  float sp;     // 1 / Mtot (physical-space normalisation of the inverse transforms)
+  float so;     // output normalisation of the forward transform (1/Ntot, or Mtot/Ntot^2 padded)
+};
+
+FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
+FIT_D float2 fz_muli(float2 h, float k) { return make_float2(-h.y * k, h.x * k); }   // i*k*h
+
+// ---- zinv --------------------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zinv(FzArgs a, const float2* __restrict__ H,
+                                                                    const uint16_t* __restrict__ sb,
+                                                                    const float* __restrict__ kd,
+                                                                    float2* __restrict__ out,
+                                                                    const float2* __restrict__ twg) {
+  typedef CtTile<float2, N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const long c0 = (long)blockIdx.z * C;
+  const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
+  const int m = a.med[b];
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += NT) {
+    const int cc = i % C, e = i / C;
+    const long col = c0 + cc;
+    const int f = fz_freq(e, N);
+    float2 val = make_float2(0.f, 0.f);
+    if (col < a.P1 && f >= -a.K && f <= a.K) {
+      const int kz = f + a.K;
+      if (sb[(long)kz * a.P1 + col] == m) {
+        val = H[((long)c * a.KY + kz) * a.P1 + col];
+        if (v) val = fz_muli(val, kd[kz]);
+      }
+    }
+    s[swz(e, cc, C)] = val;
+  }
+  __syncthreads();
+  ct_stages<float2, true, N, C, NT, TT::EPT, 0>(s, tw, tid);
+  const long ob = (((long)b * 3 + c) * 2 + v) * N;
+#pragma unroll 4
+  for (int i = tid; i < E; i += NT) {
+    const int cc = i % C, e = i / C;
+    const long col = c0 + cc;
+    if (col < a.P1) out[(ob + e) * a.P1 + col] = s[swz(e, cc, C)];
+  }
+}
+
+// ---- yinv --------------------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yinv(FzArgs a, const float2* __restrict__ in,
+                                                                    const float* __restrict__ kd,
+                                                                    float2* __restrict__ out,
+                                                                    const float2* __restrict__ twg) {
+  typedef CtTile<float2, N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const int nkt = (a.KX + C - 1) / C;
+  const int z = blockIdx.z / nkt, k0 = (blockIdx.z % nkt) * C;
+  const int c = blockIdx.y / 3, j = blockIdx.y % 3, b = blockIdx.x;
+  const int v = (j == 2) ? 1 : 0;
+  const long ib = ((((long)b * 3 + c) * 2 + v) * N + z) * a.P1;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += NT) {
+    const int cc = i % C, e = i / C;
+    const int kx = k0 + cc;
+    const int f = fz_freq(e, N);
+    float2 val = make_float2(0.f, 0.f);
+    if (kx < a.KX && f >= -a.K && f <= a.K) {
+      const int ky = f + a.K;
+      val = in[ib + kx + (long)a.KX * ky];
+      if (j == 1) val = fz_muli(val, kd[ky]);
+    }
+    s[swz(e, cc, C)] = val;
+  }
+  __syncthreads();
+  ct_stages<float2, true, N, C, NT, TT::EPT, 0>(s, tw, tid);
+  const long obase = ((((long)b * 3 + c) * 3 + j) * N + z) * N;
+#pragma unroll 4
+  for (int i = tid; i < E; i += NT) {
+    const int cc = i % C, e = i / C;
+    const int kx = k0 + cc;
+    if (kx < a.KX) out[(obase + e) * a.KX + kx] = s[swz(e, cc, C)];
+  }
+}
+
+// ---- xmix: inverse x transforms, product with the advecting velocity, forward x transform -----
+template <int N>
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_xmix(FzArgs a, const float2* __restrict__ G,
+                                                                    const float* __restrict__ U,
+                                                                    const float* __restrict__ kd,
+                                                                    float2* __restrict__ out,
+                                                                    const float2* __restrict__ twg) {
+  typedef CtTile<float2, N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
+  static_assert(NT * EPT == E, "xmix needs an exact thread/element split");
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const long l0 = (long)blockIdx.z * 2 * C;
+  const int b = blockIdx.x;
+  const long Mtot = (long)N * N * N;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  for (int c = 0; c < 3; ++c) {
+    float2 acc[EPT];
+#pragma unroll
+    for (int r = 0; r < EPT; ++r) acc[r] = make_float2(0.f, 0.f);
+    for (int j = 0; j < 3; ++j) {
+      const long gb = (((long)b * 3 + c) * 3 + j) * a.L;
+      __syncthreads();
+#pragma unroll 4
+      for (int r = 0; r < EPT; ++r) {
+        const int i = tid + r * NT;
+        const int col = i / N, k = i % N;
+        const long la = l0 + 2 * col, lb = la + 1;
+        const bool cj = 2 * k > N;
+        const int kk = cj ? N - k : k;
+        float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+        if (kk <= a.K) {
+          if (la < a.L) A = G[(gb + la) * a.KX + kk];
+          if (lb < a.L) B = G[(gb + lb) * a.KX + kk];
+          if (j == 0) {
+            const float kx = kd[a.K + kk];
+            A = fz_muli(A, kx);
+            B = fz_muli(B, kx);
+          }
+          if (cj) { A.y = -A.y; B.y = -B.y; }
+          if (k == 0) { A.y = 0.f; B.y = 0.f; }
+        }
+        s[swz(k, col, C)] = make_float2(A.x - B.y, A.y + B.x);
+      }
+      __syncthreads();
+      ct_stages<float2, true, N, C, NT, EPT, 0>(s, tw, tid);
+      const float* Uj = U + (long)j * Mtot;
+#pragma unroll 4
+      for (int r = 0; r < EPT; ++r) {
+        const int i = tid + r * NT;
+        const int col = i / N, x = i % N;
+        const long la = l0 + 2 * col, lb = la + 1;
+        const float2 zv = s[swz(x, col, C)];
+        const float ua = (la < a.L) ? Uj[la * N + x] : 0.f;
+        const float ub = (lb < a.L) ? Uj[lb * N + x] : 0.f;
+        acc[r].x += ua * (zv.x * a.sp);
+        acc[r].y += ub * (zv.y * a.sp);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < EPT; ++r) {
+      const int i = tid + r * NT;
+      const int col = i / N, x = i % N;
+      s[swz(x, col, C)] = acc[r];
+    }
+    __syncthreads();
+    ct_stages<float2, false, N, C, NT, EPT, 0>(s, tw, tid);
+    const long obase = ((long)b * 3 + c) * a.L;
+    const float hs = 0.5f * a.so;
+    for (int i = tid; i < C * a.KX; i += NT) {
+      const int col = i / a.KX, k = i % a.KX;
+      const long la = l0 + 2 * col, lb = la + 1;
+      const float2 zk = s[swz(k, col, C)];
+      const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
+      if (la < a.L) out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+      if (lb < a.L) out[(obase + lb) * a.KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+    }
+  }
+}
+
+// ---- yfwd --------------------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
+                                                                    float2* __restrict__ out,
+                                                                    const float2* __restrict__ twg) {
+  typedef CtTile<float2, N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const int nkt = (a.KX + C - 1) / C;
+  const int z = blockIdx.z / nkt, k0 = (blockIdx.z % nkt) * C;
+  const int c = blockIdx.y, b = blockIdx.x;
+  const long ib = ((long)b * 3 + c) * a.L + (long)N * z;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += NT) {
+    const int cc = i % C, e = i / C;
+    const int kx = k0 + cc;
+    s[swz(e, cc, C)] = (kx < a.KX) ? in[(ib + e) * a.KX + kx] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  ct_stages<float2, false, N, C, NT, TT::EPT, 0>(s, tw, tid);
+  const long obase = (((long)b * 3 + c) * N + z) * a.KY;
+#pragma unroll 4
+  for (int i = tid; i < E; i += NT) {
+    const int cc = i % C, e = i / C;
+    const int kx = k0 + cc;
+    const int f = fz_freq(e, N);
+    if (kx < a.KX && f >= -a.K && f <= a.K) out[(obase + f + a.K) * a.KX + kx] = s[swz(e, cc, C)];
+  }
+}
+
+// ---- zfwd + shell binning ------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
+                                                                        const float2* __restrict__ Ceff,
+                                                                        const uint16_t* __restrict__ seff,
+                                                                        double* __restrict__ partial,
+                                                                        const float2* __restrict__ twg) {
+  typedef CtTile<float2, N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
+  static_assert(NT * EPT == E, "zfwd needs an exact thread/element split");
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  double* bins = reinterpret_cast<double*>(tw + N);
+  const int tid = threadIdx.x;
+  const long c0 = (long)blockIdx.z * C;
+  const int b = blockIdx.x;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  for (int t = tid; t < a.nsh; t += NT) bins[t] = 0.0;
+  float tacc[EPT];
+#pragma unroll
+  for (int r = 0; r < EPT; ++r) tacc[r] = 0.f;
+  for (int c = 0; c < 3; ++c) {
+    const long ib = ((long)b * 3 + c) * N;
+    __syncthreads();
+#pragma unroll 4
+    for (int r = 0; r < EPT; ++r) {
+      const int i = tid + r * NT;
+      const int cc = i % C, e = i / C;
+      const long col = c0 + cc;
+      s[swz(e, cc, C)] = (col < a.P1) ? in[(ib + e) * a.P1 + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    ct_stages<float2, false, N, C, NT, EPT, 0>(s, tw, tid);
+#pragma unroll 4
+    for (int r = 0; r < EPT; ++r) {
+      const int i = tid + r * NT;
+      const int cc = i % C, e = i / C;
+      const long col = c0 + cc;
+      const int f = fz_freq(e, N);
+      if (col < a.P1 && f >= -a.K && f <= a.K) {
+        const float2 nv = s[swz(e, cc, C)];
+        const float2 cv = Ceff[((long)c * a.KY + f + a.K) * a.P1 + col];
+        tacc[r] += cv.x * nv.x + cv.y * nv.y;
+      }
+    }
+  }
+  const unsigned lane = threadIdx.x & 31;
+#pragma unroll 4
+  for (int r = 0; r < EPT; ++r) {
+    const int i = tid + r * NT;
+    const int cc = i % C, e = i / C;
+    const long col = c0 + cc;
+    const int f = fz_freq(e, N);
+    int sh = 0;
+    if (col < a.P1 && f >= -a.K && f <= a.K) sh = seff[(long)(f + a.K) * a.P1 + col];
+    const double v = sh ? (double)tacc[r] : 0.0;
+    const unsigned grp = __match_any_sync(0xffffffffu, sh);
+    double sum = 0.0;
+    for (unsigned mm = grp; mm; mm &= mm - 1) sum += __shfl_sync(grp, v, __ffs(mm) - 1);
+    if (sh && (int)lane == __ffs(grp) - 1) atomicAdd(&bins[sh - 1], sum);
+  }
+  __syncthreads();
+  double* pb = partial + ((long)b * gridDim.z + blockIdx.z) * a.nsh;
+  for (int t = tid; t < a.nsh; t += NT) pb[t] = bins[t];
+}
+
+template <typename K>
+static int ct_prep_fused(K kern, size_t smem) {
+  if (smem <= 48 * 1024) return FIT_OK;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    fit_set_error("cudaFuncSetAttribute(smem=%zu) failed: %s", smem, cudaGetErrorString(e));
+    return FIT_ERR_CUDA;
+  }
+  return FIT_OK;
+}
+
+// ---- host launcher for one batch (instantiated per transform length) -------------------------
+template <int N>
+int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff, const uint16_t* sb,
+             const float* kd, const float* U, float2* bufA, float2* bufB, double* partial, const float2* tw,
+             cudaStream_t st) {
+  typedef CtTile<float2, N> TT;
+  constexpr int C = TT::C;
+  const size_t sm = TT::SMEM;
+  const size_t smb = TT::SMEM + sizeof(double) * a.nsh + 16;
+  FIT_TRY(ct_prep_fused(k_fz_zinv<N>, sm));
+  FIT_TRY(ct_prep_fused(k_fz_yinv<N>, sm));
+  FIT_TRY(ct_prep_fused(k_fz_xmix<N>, sm));
+  FIT_TRY(ct_prep_fused(k_fz_yfwd<N>, sm));
+  FIT_TRY(ct_prep_fused(k_fz_zfwd_bin<N>, smb));
+  const unsigned pt = (unsigned)((a.P1 + C - 1) / C);
+  const unsigned nkt = (unsigned)((a.KX + C - 1) / C);
+  const double cpx = 8.0;
+  fit_prof_begin(PK_S2S_ZINV, cpx * a.nb * (3.0 * a.KY * a.P1 + 6.0 * N * a.P1) + 2.0 * a.nb * a.KY * a.P1, st);
+  k_fz_zinv<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, sb, kd, bufA, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_YINV, cpx * a.nb * (6.0 * N * a.P1 + 9.0 * (double)N * N * a.KX), st);
+  k_fz_yinv<N><<<dim3(a.nb, 9, nkt * N), TT::NTHR, sm, st>>>(a, bufA, kd, bufB, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_XMIX,
+                 cpx * a.nb * (9.0 * (double)N * N * a.KX + 3.0 * (double)N * N * a.KX) + 4.0 * 3.0 * N * N * N, st);
+  k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, sm, st>>>(a, bufB, U, kd, bufA, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_YFWD, cpx * a.nb * (3.0 * (double)N * N * a.KX + 3.0 * N * a.P1), st);
+  k_fz_yfwd<N><<<dim3(a.nb, 3, nkt * N), TT::NTHR, sm, st>>>(a, bufA, bufB, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_ZFWD_BIN, cpx * (a.nb * 3.0 * N * a.P1 + 3.0 * a.KY * a.P1) + 2.0 * a.KY * a.P1, st);
+  k_fz_zfwd_bin<N><<<dim3(a.nb, 1, pt), TT::NTHR, smb, st>>>(a, bufB, Ceff, seff, partial, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+}  // namespace fit

@@ -4,13 +4,22 @@
 //
 // Shells with no retained mode contribute an exactly-zero column (the reference transforms
 // zero fields), so they are skipped. The advecting velocity is transformed once per call.
+#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
 
+#include "fit_fused_impl.cuh"
 #include "fit_plan.cuh"
 
 namespace fit {
+
+int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
+                  const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
+                  const float2* tw, cudaStream_t st);
+int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
+                  const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
+                  const float2* tw, cudaStream_t st);
 
 struct S2SState {
   cudaGraphExec_t exec = nullptr;
@@ -25,13 +34,18 @@ struct S2SState {
   const double* key_T = nullptr;
   std::vector<int> occ;   // retained modes per shell
   fit_dbuf occ_dev;
+  // fused-path buffers
+  fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart;
+  int fkd_n = -1;
 };
 
 void s2s_free(fit_plan* p) {
   S2SState* s = (S2SState*)p->s2s;
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
-  if (s->occ_dev.p) cudaFree(s->occ_dev.p);
+  fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse, &s->fsb, &s->fkd, &s->fA, &s->fB, &s->fpart};
+  for (fit_dbuf* b : bufs)
+    if (b->p) cudaFree(b->p);
   delete s;
   p->s2s = nullptr;
 }
@@ -135,6 +149,172 @@ static int run_batched(fit_plan* p, S2SState* s, const void* ud, const void* ad,
   return FIT_OK;
 }
 
+// ---- fused FP32 path (cubic 3D grids, 2/3 or 3/2) -------------------------------------------------
+
+static bool fused_size(int M) {
+  return M == 64 || M == 96 || M == 128 || M == 192 || M == 256 || M == 384 || M == 512 || M == 768;
+}
+
+static bool fused_ok(const fit_plan* p) {
+  const char* env = getenv("FIT_NO_FUSED");
+  if (env && env[0] == '1') return false;
+  const GridDesc& g = p->g;
+  if (g.nd != 3 || p->prec != 32 || p->M != 3 || p->Dadv < 3) return false;
+  if (p->dealias != 1 && p->dealias != 2) return false;
+  if (g.N[0] != g.N[1] || g.N[0] != g.N[2] || !fused_size(g.M[0])) return false;
+  return p->ks_host[0] == p->ks_host[1] && p->ks_host[0] == p->ks_host[2];
+}
+
+static int ct_cols32(int N) {   // CtTile<float2, N>::C
+  int w = 1;
+  while (w * 2 <= 4096 / N) w *= 2;
+  return w > 16 ? w : 16;
+}
+
+// H (Hermitian part of the masked / embedded velocity), band shell, effective carrier and
+// binning shell for every live half-spectrum mode, compact layout [c][kz'][kx + KX ky'].
+__global__ void k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, const void* F, int f64, int inv,
+                           int two_thirds, const uint16_t* __restrict__ shell, float2* H, float2* Ceff,
+                           uint16_t* seff, uint16_t* sb) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= P1 * KY) return;
+  const long col = i % P1;
+  const int kz = (int)(i / P1);
+  const int kx = (int)(col % KX), ky = (int)(col / KX);
+  KIdx kA, kB;
+  map_pair(g, kx, fmod_pos(ky - K, g.M[1]), fmod_pos(kz - K, g.M[2]), &kA, &kB);
+  const bool okA = kA.lin >= 0 && (!two_thirds || keep23(g, kA.k));
+  const bool okB = kB.lin >= 0 && (!two_thirds || keep23(g, kB.k));
+  for (int c = 0; c < 3; ++c) {
+    double2 acc = make_double2(0, 0);
+    if (okA) { const double2 v = ld_c(F, f64, kA.lin + g.Ntot * c); acc.x += v.x; acc.y += v.y; }
+    if (okB) { const double2 v = ld_c(F, f64, kB.lin + g.Ntot * c); acc.x += v.x; acc.y -= v.y; }
+    H[((long)c * KY + kz) * P1 + col] = make_float2((float)(0.5 * acc.x), (float)(0.5 * acc.y));
+  }
+  sb[(long)kz * P1 + col] = kA.lin >= 0 ? shell[kA.lin] : (kB.lin >= 0 ? shell[kB.lin] : 0);
+  const bool A = kA.lin >= 0;
+  const bool B = kB.lin >= 0 && kx >= 1 && (g.padded ? true : (2 * kx < g.N[0]));
+  uint16_t sh = A ? shell[kA.lin] : (B ? shell[kB.lin] : 0);
+  if (two_thirds && (A || B) && !keep23(g, A ? kA.k : kB.k)) sh = 0;
+  double2 CA[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+  double2 CB[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+  if (sh) {
+    if (A) carrier_at(g, kt, F, f64, g.Ntot, 3, inv, kA.lin, kA.k, CA);
+    if (B) carrier_at(g, kt, F, f64, g.Ntot, 3, inv, kB.lin, kB.k, CB);
+  }
+  for (int c = 0; c < 3; ++c)
+    Ceff[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
+  seff[(long)kz * P1 + col] = sh;
+}
+
+__global__ void k_fz_reduce(const double* __restrict__ partial, int npt, FzArgs a, double* Td) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.nb * a.nsh) return;
+  const int b = j / a.nsh, n = j % a.nsh;
+  double s = 0.0;
+  for (int t = 0; t < npt; ++t) s += partial[((long)b * npt + t) * a.nsh + n];
+  Td[(long)(a.med[b] - 1) * a.nsh + n] = s;
+}
+
+static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {
+  const GridDesc& g = p->g;
+  const int N = g.N[0], M = g.M[0], nsh = p->nsh;
+  const int K = (p->dealias == 1) ? N / 3 - 1 : N / 2;
+  const int KX = K + 1, KY = 2 * K + 1;
+  const long P1 = (long)KX * KY, L = (long)M * M;
+  const int C = ct_cols32(M);
+  const long npt = (P1 + C - 1) / C;
+  const double perA = (double)(6.0 * M * P1 > 3.0 * L * KX ? 6.0 * M * P1 : 3.0 * L * KX);
+  const double perB = (double)(9.0 * L * KX > 3.0 * M * P1 ? 9.0 * L * KX : 3.0 * M * P1);
+  int B = (int)(40e9 / (8.0 * (perA + perB)));
+  if (B > 16) B = 16;
+  if (B < 1) B = 1;
+  FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 3 * KY * P1));
+  FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * KY * P1));
+  FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * KY * P1));
+  FIT_TRY(ensure(p, &s->fsb, sizeof(uint16_t) * KY * P1));
+  FIT_TRY(ensure(p, &s->fkd, sizeof(float) * KY));
+  FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA * B)));
+  FIT_TRY(ensure(p, &s->fB, (size_t)(8.0 * perB * B)));
+  FIT_TRY(ensure(p, &s->fpart, sizeof(double) * (size_t)B * npt * nsh));
+  FIT_TRY(ensure(p, &p->hs, sizeof(float2) * 3 * g.Mhalf));
+  FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
+  if (s->fkd_n != KY) {   // derivative multipliers of the live indices (never during capture)
+    std::vector<float> kd(KY);
+    const std::vector<double>& ks = p->ks_host[0];
+    for (int i = 0; i < KY; ++i) {
+      const int f = i - K;
+      double v = ks[((f % N) + N) % N];
+      if (g.padded && 2 * f == N) v = -ks[N / 2];   // padded +N/2 mirrors the data-grid Nyquist
+      kd[i] = (float)v;
+    }
+    FIT_CUDA_CHECK(cudaMemcpy(s->fkd.p, kd.data(), sizeof(float) * KY, cudaMemcpyHostToDevice));
+    s->fkd_n = KY;
+  }
+  float2* H = (float2*)s->fH.p;
+  float2* Ce = (float2*)s->fC.p;
+  uint16_t* se = (uint16_t*)s->fse.p;
+  uint16_t* sbp = (uint16_t*)s->fsb.p;
+  const long nset = P1 * KY;
+  fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
+  k_fz_setup<<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv,
+                                                                    p->dealias == 1, (const uint16_t*)p->shell_full.p,
+                                                                    H, Ce, se, sbp);
+  fit_prof_end(p->stream);
+  FIT_LAUNCH_CHECK();
+  // advecting velocity in physical space (once per call)
+  GatherArgs ga;
+  memset(&ga, 0, sizeof(ga));
+  ga.src[0] = ud;
+  ga.src[1] = ad;
+  ga.src_comp_stride[0] = g.Ntot;
+  ga.src_comp_stride[1] = g.Ntot;
+  ga.in_f64 = p->io_f64;
+  ga.two_thirds = p->dealias == 1;
+  ga.scale = 1.0;
+  ga.nfields = 3;
+  for (int j = 0; j < 3; ++j) ga.f[j] = GatherField{1, j, -1, 0};
+  FIT_TRY(gather_half<float>(g, p->kt, ga, (float2*)p->hs.p, p->stream));
+  FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)(1.0 / (double)g.Mtot),
+                            p->stream));
+  std::vector<int> meds;
+  for (int m = 1; m <= nsh; ++m)
+    if (s->occ[m - 1] > 0) meds.push_back(m);
+  FzArgs a;
+  memset(&a, 0, sizeof(a));
+  a.K = K;
+  a.KX = KX;
+  a.KY = KY;
+  a.P1 = P1;
+  a.L = L;
+  a.nsh = nsh;
+  a.sp = (float)(1.0 / (double)g.Mtot);
+  a.so = (float)(g.padded ? (double)g.Mtot / ((double)g.Ntot * (double)g.Ntot) : 1.0 / (double)g.Ntot);
+  const float2* tw = p->ax[0].tw32;
+  for (size_t b0 = 0; b0 < meds.size(); b0 += B) {
+    a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
+    for (int b = 0; b < a.nb; ++b) a.med[b] = meds[b0 + b];
+    int rc = fz_dispatch_a(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
+                           (float2*)s->fB.p, (double*)s->fpart.p, tw, p->stream);
+    if (rc == 1)
+      rc = fz_dispatch_b(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
+                         (float2*)s->fB.p, (double*)s->fpart.p, tw, p->stream);
+    if (rc != FIT_OK) {
+      if (rc == 1) fit_set_error("no fused kernels for size %d", M);
+      return rc == 1 ? FIT_ERR_SIZE : rc;
+    }
+    k_fz_reduce<<<(unsigned)((a.nb * nsh + 127) / 128), 128, 0, p->stream>>>((const double*)s->fpart.p, (int)npt, a,
+                                                                              Td);
+    FIT_LAUNCH_CHECK();
+  }
+  return FIT_OK;
+}
+
+static int run_s2s(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {
+  if (fused_ok(p)) return run_fused(p, s, ud, ad, inv, Td);
+  return (p->prec == 64) ? run_batched<double>(p, s, ud, ad, inv, Td) : run_batched<float>(p, s, ud, ad, inv, Td);
+}
+
 int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td) {
   S2SState* s = (S2SState*)p->s2s;
   if (!s) {
@@ -159,7 +339,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
     FIT_CUDA_CHECK(cudaMemcpyAsync(s->occ.data(), s->occ_dev.p, sizeof(int) * p->nsh, cudaMemcpyDeviceToHost, p->stream));
     FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));
     // first call for this key: run eagerly (allocates the workspace, sets kernel attributes)
-    const int rc = (p->prec == 64) ? run_batched<double>(p, s, ud, ad, inv, Td) : run_batched<float>(p, s, ud, ad, inv, Td);
+    const int rc = run_s2s(p, s, ud, ad, inv, Td);
     if (rc != FIT_OK) return rc;
     s->key_u = ud;
     s->key_a = ad;
@@ -172,7 +352,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
     return FIT_OK;
   }
   if (fit_prof_on()) {   // per-launch events need eager launches
-    return (p->prec == 64) ? run_batched<double>(p, s, ud, ad, inv, Td) : run_batched<float>(p, s, ud, ad, inv, Td);
+    return run_s2s(p, s, ud, ad, inv, Td);
   }
   if (s->exec) {
     FIT_CUDA_CHECK(cudaGraphLaunch(s->exec, p->stream));
@@ -183,7 +363,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
   cudaGraph_t graph = nullptr;
   FIT_CUDA_CHECK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
   const long before = fit_launch_total();
-  int rc = (p->prec == 64) ? run_batched<double>(p, s, ud, ad, inv, Td) : run_batched<float>(p, s, ud, ad, inv, Td);
+  int rc = run_s2s(p, s, ud, ad, inv, Td);
   const long captured = fit_launch_total() - before;
   cudaError_t ce = cudaStreamEndCapture(p->stream, &graph);
   fit_count_launches(-captured);

@@ -221,3 +221,20 @@ def test_zero_field_gives_zero():
     r = F.calculate_shell_to_shell_transfer(np.zeros((6, 6, 2), complex), ks, binning=F.LinearBinning(1.0),
                                             dealiasing=F.NoDealiasing(), verify_antisymmetry=False)
     assert np.all(np.abs(r.transfer_matrix) < 1e-14) and np.isnan(r.max_antisymmetry_error)
+
+
+@pytest.mark.parametrize("deal", ["two_thirds", "three_halves"])
+@pytest.mark.parametrize("inv", ["ke", "helicity"])
+@pytest.mark.parametrize("herm", [True, False])
+def test_fused_shell_to_shell_64(deal, inv, herm):
+    """The fused FP32 pipeline (cubic grid of a compiled size) against the FP64 oracle."""
+    if herm:
+        u, ks = spectrum_field((64, 64, 64), e_config2, seed=5)
+    else:
+        u, ks = curl_noise_3d(64, 6)
+    I = {"ke": F.KineticEnergy(), "helicity": F.Helicity()}[inv]
+    r = F.calculate_shell_to_shell_transfer(u, ks, binning=F.LinearBinning(4.0), dealiasing=DEAL[deal], invariant=I,
+                                            spectral=F.GB300Spectral(32), execution=F.GB300Execution("batched"))
+    _, _, T, net, _ = O.shell_to_shell(u, ks, ("linear", 4.0), deal, inv)
+    assert rel(r.transfer_matrix, T) < 1e-5
+    assert rel(r.net_transfer, net) < 1e-4
