@@ -526,6 +526,7 @@ int fit_shell_to_shell(fit_plan* p, const void* u_hat, const void* adv_hat, cons
   FIT_CUDA_CHECK(cudaMemsetAsync(Td, 0, sizeof(double) * (size_t)nsh * nsh, p->stream));
   if (mode == FIT_S2S_BATCHED) {
     FIT_TRY(s2s_batched(p, ud, ad, invariant, Td));
+    FIT_TRY(s2s_check(p));
   } else if (p->prec == 64) {
     FIT_TRY(carrier_and_bin_setup<double>(p, ud, invariant));
     for (int m = 1; m <= nsh; ++m) {

@@ -304,7 +304,9 @@ __host__ __device__ constexpr int ct_nst(int N) {
   while (n % 5 == 0) { n /= 5; ++c; }
   return c;
 }
-__host__ __device__ constexpr int ct_radix(int N, int s) {
+// Radix schedule: 8s, then 4 or 2, then 3s, then 5s; when there are two or more 8s, one 8 moves
+// to the end so the first and last stages share a radix (see ct_fft_mapped).
+__host__ __device__ constexpr int ct_radix_raw(int N, int s) {
   const int p2 = ct_p2(N), n8 = p2 / 3, rem = p2 % 3;
   if (s < n8) return 8;
   int idx = n8;
@@ -316,6 +318,14 @@ __host__ __device__ constexpr int ct_radix(int N, int s) {
   while (n % 3 == 0) { n /= 3; ++n3; }
   if (s < idx + n3) return 3;
   return 5;
+}
+__host__ __device__ constexpr int ct_radix(int N, int s) {
+  const int nst = ct_nst(N), n8 = ct_p2(N) / 3;
+  if (n8 >= 2 && ct_radix_raw(N, nst - 1) != 8) {
+    if (s == nst - 1) return 8;
+    return ct_radix_raw(N, s < n8 - 1 ? s : s + 1);
+  }
+  return ct_radix_raw(N, s);
 }
 __host__ __device__ constexpr int ct_span(int N, int s) { int p = 1; for (int i = 0; i < s; ++i) p *= ct_radix(N, i); return p; }
 __host__ __device__ constexpr int ct_pow2floor(int x) { int p = 1; while (p * 2 <= x) p *= 2; return p; }
@@ -493,6 +503,96 @@ __global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_r2c_x(const typename 
     const V zn = s[swz(k == 0 ? 0 : N - k, c, C)];
     if (a < L) out[a * Nh + k] = mkc<V>((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
     if (b < L) out[b * Nh + k] = mkc<V>((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+  }
+}
+
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, int SEND>
+__device__ __forceinline__ void ct_stages_range(V* s, const V* tw, int tid) {
+  if constexpr (S < SEND) {
+    ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S)>(s, tw, tid);
+    ct_stages_range<V, INV, N, C, NTHR, EPT, S + 1, SEND>(s, tw, tid);
+  }
+}
+
+// Element map shared by a transform's inputs and outputs: butterfly b = tid + i*NTHR of the last
+// stage (radix RL) owns column b % C and rows j + q*NRL, j = b / C, q < RL.
+template <int N>
+struct CtMap {
+  static constexpr int NST = ct_nst(N);
+  static constexpr int RL = ct_radix(N, NST - 1);
+  static constexpr int NRL = N / RL;
+  static constexpr bool DIRECT = NST >= 2 && ct_radix(N, 0) == RL;
+};
+
+// Transform of a C-column tile whose inputs come from load(i, q, row, col) and whose outputs go to
+// store(i, q, row, col, value), both on the CtMap element map. When the first and last stages share
+// a radix (DIRECT), stage 0 runs on the loaded registers and the last stage hands its registers to
+// store, so only the inner stage exchanges touch shared memory; otherwise the map is staged through
+// shared memory around the full stage sequence. store may write the element it receives back into s
+// (each thread only rewrites rows it just read). Callers synchronise before reusing s.
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, typename LD, typename ST>
+__device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD load, ST store) {
+  typedef CtMap<N> MP;
+  constexpr int RL = MP::RL, NRL = MP::NRL;
+  constexpr int MB = (EPT + RL - 1) / RL;
+  constexpr int NB = C * NRL;
+  V v[MB][RL];
+  if constexpr (MP::DIRECT) {
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) v[i][q] = load(i, q, j + q * NRL, c);
+        dftr<V, RL, INV>(v[i]);
+#pragma unroll
+        for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+      }
+    }
+    __syncthreads();
+    ct_stages_range<V, INV, N, C, NTHR, EPT, 1, MP::NST - 1>(s, tw, tid);
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) {
+          V x = s[swz(j + q * NRL, c, C)];
+          if (q > 0) {
+            V w = tw[j * q];
+            if (INV) w.y = -w.y;
+            x = cmul(x, w);
+          }
+          v[i][q] = x;
+        }
+        dftr<V, RL, INV>(v[i]);
+#pragma unroll
+        for (int q = 0; q < RL; ++q) store(i, q, j + q * NRL, c, v[i][q]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) s[swz(j + q * NRL, c, C)] = load(i, q, j + q * NRL, c);
+      }
+    }
+    __syncthreads();
+    ct_stages<V, INV, N, C, NTHR, EPT, 0>(s, tw, tid);
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) store(i, q, j + q * NRL, c, s[swz(j + q * NRL, c, C)]);
+      }
+    }
   }
 }
 

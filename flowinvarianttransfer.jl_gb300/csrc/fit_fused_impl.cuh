@@ -24,6 +24,7 @@
 
 #include "fit_fft.cuh"
 #include "fit_maps.cuh"
+#include "fit_tma.cuh"
 
 namespace fit {
 
@@ -58,30 +59,27 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zinv(FzArgs a, c
   const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
   const int m = a.med[b];
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-#pragma unroll 4
-  for (int i = tid; i < E; i += NT) {
-    const int cc = i % C, e = i / C;
-    const long col = c0 + cc;
-    const int f = fz_freq(e, N);
-    float2 val = make_float2(0.f, 0.f);
-    if (col < a.P1 && f >= -a.K && f <= a.K) {
-      const int kz = f + a.K;
-      if (sb[(long)kz * a.P1 + col] == m) {
-        val = H[((long)c * a.KY + kz) * a.P1 + col];
-        if (v) val = fz_muli(val, kd[kz]);
-      }
-    }
-    s[swz(e, cc, C)] = val;
-  }
   __syncthreads();
-  ct_stages<float2, true, N, C, NT, TT::EPT, 0>(s, tw, tid);
   const long ob = (((long)b * 3 + c) * 2 + v) * N;
-#pragma unroll 4
-  for (int i = tid; i < E; i += NT) {
-    const int cc = i % C, e = i / C;
-    const long col = c0 + cc;
-    if (col < a.P1) out[(ob + e) * a.P1 + col] = s[swz(e, cc, C)];
-  }
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const long col = c0 + cc;
+        const int f = fz_freq(e, N);
+        float2 val = make_float2(0.f, 0.f);
+        if (col < a.P1 && f >= -a.K && f <= a.K) {
+          const int kz = f + a.K;
+          if (sb[(long)kz * a.P1 + col] == m) {
+            val = H[((long)c * a.KY + kz) * a.P1 + col];
+            if (v) val = fz_muli(val, kd[kz]);
+          }
+        }
+        return val;
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const long col = c0 + cc;
+        if (col < a.P1) out[(ob + e) * a.P1 + col] = val;
+      });
 }
 
 // ---- yinv --------------------------------------------------------------------------------------
@@ -102,28 +100,25 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yinv(FzArgs a, c
   const int v = (j == 2) ? 1 : 0;
   const long ib = ((((long)b * 3 + c) * 2 + v) * N + z) * a.P1;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-#pragma unroll 4
-  for (int i = tid; i < E; i += NT) {
-    const int cc = i % C, e = i / C;
-    const int kx = k0 + cc;
-    const int f = fz_freq(e, N);
-    float2 val = make_float2(0.f, 0.f);
-    if (kx < a.KX && f >= -a.K && f <= a.K) {
-      const int ky = f + a.K;
-      val = in[ib + kx + (long)a.KX * ky];
-      if (j == 1) val = fz_muli(val, kd[ky]);
-    }
-    s[swz(e, cc, C)] = val;
-  }
   __syncthreads();
-  ct_stages<float2, true, N, C, NT, TT::EPT, 0>(s, tw, tid);
   const long obase = ((((long)b * 3 + c) * 3 + j) * N + z) * N;
-#pragma unroll 4
-  for (int i = tid; i < E; i += NT) {
-    const int cc = i % C, e = i / C;
-    const int kx = k0 + cc;
-    if (kx < a.KX) out[(obase + e) * a.KX + kx] = s[swz(e, cc, C)];
-  }
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const int kx = k0 + cc;
+        const int f = fz_freq(e, N);
+        float2 val = make_float2(0.f, 0.f);
+        if (kx < a.KX && f >= -a.K && f <= a.K) {
+          const int ky = f + a.K;
+          val = in[ib + kx + (long)a.KX * ky];
+          if (j == 1) val = fz_muli(val, kd[ky]);
+        }
+        return val;
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const int kx = k0 + cc;
+        if (kx < a.KX) out[(obase + e) * a.KX + kx] = val;
+      });
 }
 
 // ---- xmix: inverse x transforms, product with the advecting velocity, forward x transform -----
@@ -209,6 +204,141 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_xmix(FzArgs a, c
   }
 }
 
+// ---- xmix with bulk-copy staging ------------------------------------------------------------------
+// Same arithmetic as k_fz_xmix. The nine gradient tiles a block consumes ((c, j) pairs; each tile is
+// 2C consecutive lines x KX complex, one contiguous block of G) are streamed into two shared
+// staging buffers by bulk asynchronous copies: tile t+1 is in flight while tile t is transformed.
+// The advecting-velocity values a thread multiplies are loaded into registers before each inverse
+// transform, so their latency overlaps the transform. C = 8 columns keeps registers below the
+// two-blocks-per-SM limit.
+template <int N>
+struct XTile {
+  static constexpr int Cw = ct_pow2floor(2048 / N > 0 ? 2048 / N : 1);
+  static constexpr int C = Cw > 8 ? Cw : 8;
+  static constexpr int E = C * N;
+  static constexpr int EPT = E <= 8192 ? 8 : 16;
+  static constexpr int NTHR = E / EPT;
+  static constexpr size_t SMEM_FIXED = (((size_t)(E + N) * 8 + 16) + 127) / 128 * 128;
+};
+
+template <int N>
+__global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, const float2* __restrict__ G,
+                                                                const float* __restrict__ U,
+                                                                const float* __restrict__ kd,
+                                                                float2* __restrict__ out,
+                                                                const float2* __restrict__ twg, int* err) {
+  typedef XTile<N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
+  static_assert(NT * EPT == E, "xmix needs an exact thread/element split");
+  extern __shared__ __align__(128) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + N);
+  float2* stg = reinterpret_cast<float2*>(fit_smem_raw + TT::SMEM_FIXED);
+  const int SB = 2 * C * a.KX;
+  const uint32_t bytes = (uint32_t)SB * 8u;
+  const int tid = threadIdx.x;
+  const long l0 = (long)blockIdx.z * 2 * C;
+  const int b = blockIdx.x;
+  const long Mtot = (long)N * N * N;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+  }
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  if (tid == 0) {
+    const long gb = ((long)b * 3 * 3) * a.L;
+    mbar_expect_tx(&bar[0], bytes);
+    bulk_g2s(stg, G + (gb + l0) * a.KX, bytes, &bar[0]);
+  }
+  float2 acc[EPT];
+  for (int t = 0; t < 9; ++t) {
+    const int c = t / 3, j = t % 3, buf = t & 1;
+    if (j == 0) {
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) acc[r] = make_float2(0.f, 0.f);
+    }
+    if (tid == 0 && t + 1 < 9) {
+      const int c1 = (t + 1) / 3, j1 = (t + 1) % 3, nb1 = (t + 1) & 1;
+      const long gb = (((long)b * 3 + c1) * 3 + j1) * a.L;
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[nb1], bytes);
+      bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KX, bytes, &bar[nb1]);
+    }
+    // advecting velocity at this thread's accumulate positions (lanes along x: coalesced), loaded
+    // ahead of the transform so the loads overlap it
+    const float* Uj = U + (long)j * Mtot;
+    float ua[EPT], ub[EPT];
+#pragma unroll
+    for (int r = 0; r < EPT; ++r) {
+      const int i = tid + r * NT;
+      const int col = i / N, x = i % N;
+      const long la = l0 + 2 * col;
+      ua[r] = Uj[la * N + x];
+      ub[r] = Uj[(la + 1) * N + x];
+    }
+    const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(err, 1);
+      return;
+    }
+    const float2* sg = stg + buf * SB;
+    ct_fft_mapped<float2, true, N, C, NT, EPT>(
+        s, tw, tid,
+        [&](int, int, int k, int col) -> float2 {
+          const bool cj = 2 * k > N;
+          const int kk = cj ? N - k : k;
+          float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+          if (kk <= a.K) {
+            A = sg[(2 * col) * a.KX + kk];
+            B = sg[(2 * col + 1) * a.KX + kk];
+            if (j == 0) {
+              const float kx = kd[a.K + kk];
+              A = fz_muli(A, kx);
+              B = fz_muli(B, kx);
+            }
+            if (cj) { A.y = -A.y; B.y = -B.y; }
+            if (k == 0) { A.y = 0.f; B.y = 0.f; }
+          }
+          return make_float2(A.x - B.y, A.y + B.x);
+        },
+        [&](int, int, int x, int col, float2 zv) { s[swz(x, col, C)] = zv; });
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < EPT; ++r) {
+      const int i = tid + r * NT;
+      const int col = i / N, x = i % N;
+      const float2 zv = s[swz(x, col, C)];
+      acc[r].x += ua[r] * (zv.x * a.sp);
+      acc[r].y += ub[r] * (zv.y * a.sp);
+    }
+    __syncthreads();
+    if (j == 2) {
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) {
+        const int i = tid + r * NT;
+        const int col = i / N, x = i % N;
+        s[swz(x, col, C)] = acc[r];
+      }
+      __syncthreads();
+      ct_stages<float2, false, N, C, NT, EPT, 0>(s, tw, tid);
+      const long obase = ((long)b * 3 + c) * a.L;
+      const float hs = 0.5f * a.so;
+      for (int i = tid; i < C * a.KX; i += NT) {
+        const int col = i / a.KX, k = i % a.KX;
+        const long la = l0 + 2 * col, lb = la + 1;
+        const float2 zk = s[swz(k, col, C)];
+        const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
+        out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+        out[(obase + lb) * a.KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // ---- yfwd --------------------------------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
@@ -225,25 +355,27 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yfwd(FzArgs a, c
   const int c = blockIdx.y, b = blockIdx.x;
   const long ib = ((long)b * 3 + c) * a.L + (long)N * z;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-#pragma unroll 4
-  for (int i = tid; i < E; i += NT) {
-    const int cc = i % C, e = i / C;
-    const int kx = k0 + cc;
-    s[swz(e, cc, C)] = (kx < a.KX) ? in[(ib + e) * a.KX + kx] : make_float2(0.f, 0.f);
-  }
   __syncthreads();
-  ct_stages<float2, false, N, C, NT, TT::EPT, 0>(s, tw, tid);
   const long obase = (((long)b * 3 + c) * N + z) * a.KY;
-#pragma unroll 4
-  for (int i = tid; i < E; i += NT) {
-    const int cc = i % C, e = i / C;
-    const int kx = k0 + cc;
-    const int f = fz_freq(e, N);
-    if (kx < a.KX && f >= -a.K && f <= a.K) out[(obase + f + a.K) * a.KX + kx] = s[swz(e, cc, C)];
-  }
+  ct_fft_mapped<float2, false, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const int kx = k0 + cc;
+        return (kx < a.KX) ? in[(ib + e) * a.KX + kx] : make_float2(0.f, 0.f);
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const int kx = k0 + cc;
+        const int f = fz_freq(e, N);
+        if (kx < a.KX && f >= -a.K && f <= a.K) out[(obase + f + a.K) * a.KX + kx] = val;
+      });
 }
 
 // ---- zfwd + shell binning ------------------------------------------------------------------------
+// After each component's transform, thread t reads the EPT contiguous kz rows
+// [seg*EPT, seg*EPT + EPT) of pencil column t % C (seg = t / C): a warp covers two rows of all C
+// columns per access (conflict-free under the swizzle), and along a pencil the shell index changes
+// rarely, so each thread keeps a running (shell, sum) pair and flushes it to the block's FP64
+// shared-memory bins only when the shell changes.
 template <int N>
 __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
                                                                         const float2* __restrict__ Ceff,
@@ -252,7 +384,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zfwd_bin(FzArgs 
                                                                         const float2* __restrict__ twg) {
   typedef CtTile<float2, N> TT;
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
-  static_assert(NT * EPT == E, "zfwd needs an exact thread/element split");
+  static_assert(NT * EPT == E && (NT / C) * EPT == N, "zfwd needs an exact thread/element split");
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
   float2* tw = s + E;
@@ -260,6 +392,8 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zfwd_bin(FzArgs 
   const int tid = threadIdx.x;
   const long c0 = (long)blockIdx.z * C;
   const int b = blockIdx.x;
+  const int mycol = tid % C, seg = tid / C;
+  const long col = c0 + mycol;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   for (int t = tid; t < a.nsh; t += NT) bins[t] = 0.0;
   float tacc[EPT];
@@ -268,43 +402,41 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zfwd_bin(FzArgs 
   for (int c = 0; c < 3; ++c) {
     const long ib = ((long)b * 3 + c) * N;
     __syncthreads();
-#pragma unroll 4
-    for (int r = 0; r < EPT; ++r) {
-      const int i = tid + r * NT;
-      const int cc = i % C, e = i / C;
-      const long col = c0 + cc;
-      s[swz(e, cc, C)] = (col < a.P1) ? in[(ib + e) * a.P1 + col] : make_float2(0.f, 0.f);
-    }
+    ct_fft_mapped<float2, false, N, C, NT, EPT>(
+        s, tw, tid,
+        [&](int, int, int e, int cc) -> float2 {
+          const long cl = c0 + cc;
+          return (cl < a.P1) ? in[(ib + e) * a.P1 + cl] : make_float2(0.f, 0.f);
+        },
+        [&](int, int, int e, int cc, float2 val) { s[swz(e, cc, C)] = val; });
     __syncthreads();
-    ct_stages<float2, false, N, C, NT, EPT, 0>(s, tw, tid);
-#pragma unroll 4
+#pragma unroll
     for (int r = 0; r < EPT; ++r) {
-      const int i = tid + r * NT;
-      const int cc = i % C, e = i / C;
-      const long col = c0 + cc;
+      const int e = seg * EPT + r;
       const int f = fz_freq(e, N);
       if (col < a.P1 && f >= -a.K && f <= a.K) {
-        const float2 nv = s[swz(e, cc, C)];
+        const float2 nv = s[swz(e, mycol, C)];
         const float2 cv = Ceff[((long)c * a.KY + f + a.K) * a.P1 + col];
         tacc[r] += cv.x * nv.x + cv.y * nv.y;
       }
     }
   }
-  const unsigned lane = threadIdx.x & 31;
-#pragma unroll 4
+  int cur = 0;
+  double sum = 0.0;
+#pragma unroll
   for (int r = 0; r < EPT; ++r) {
-    const int i = tid + r * NT;
-    const int cc = i % C, e = i / C;
-    const long col = c0 + cc;
+    const int e = seg * EPT + r;
     const int f = fz_freq(e, N);
     int sh = 0;
     if (col < a.P1 && f >= -a.K && f <= a.K) sh = seff[(long)(f + a.K) * a.P1 + col];
-    const double v = sh ? (double)tacc[r] : 0.0;
-    const unsigned grp = __match_any_sync(0xffffffffu, sh);
-    double sum = 0.0;
-    for (unsigned mm = grp; mm; mm &= mm - 1) sum += __shfl_sync(grp, v, __ffs(mm) - 1);
-    if (sh && (int)lane == __ffs(grp) - 1) atomicAdd(&bins[sh - 1], sum);
+    if (sh != cur) {
+      if (cur) atomicAdd(&bins[cur - 1], sum);
+      cur = sh;
+      sum = 0.0;
+    }
+    if (sh) sum += (double)tacc[r];
   }
+  if (cur) atomicAdd(&bins[cur - 1], sum);
   __syncthreads();
   double* pb = partial + ((long)b * gridDim.z + blockIdx.z) * a.nsh;
   for (int t = tid; t < a.nsh; t += NT) pb[t] = bins[t];
@@ -325,7 +457,7 @@ static int ct_prep_fused(K kern, size_t smem) {
 template <int N>
 int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff, const uint16_t* sb,
              const float* kd, const float* U, float2* bufA, float2* bufB, double* partial, const float2* tw,
-             cudaStream_t st) {
+             int* err, cudaStream_t st) {
   typedef CtTile<float2, N> TT;
   constexpr int C = TT::C;
   const size_t sm = TT::SMEM;
@@ -348,7 +480,19 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_XMIX,
                  cpx * a.nb * (9.0 * (double)N * N * a.KX + 3.0 * (double)N * N * a.KX) + 4.0 * 3.0 * N * N * N, st);
-  k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, sm, st>>>(a, bufB, U, kd, bufA, tw);
+  {
+    typedef XTile<N> XT;
+    const size_t smx = XT::SMEM_FIXED + 2 * (size_t)(2 * XT::C * a.KX) * 8;
+    const bool bulk = smx <= 227 * 1024 && (a.L % (2 * XT::C)) == 0;   // 16-byte alignment holds: L, 2C are multiples of 16
+    if (bulk) {
+      FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx));
+      k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, bufB, U, kd, bufA, tw,
+                                                                                             err);
+    } else {
+      k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, sm, st>>>(a, bufB, U, kd, bufA,
+                                                                                                tw);
+    }
+  }
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_YFWD, cpx * a.nb * (3.0 * (double)N * N * a.KX + 3.0 * N * a.P1), st);

@@ -50,6 +50,7 @@ int ensure_shells(fit_plan* p, const double* edges, int n_edges, unsigned dims, 
 template <typename T>
 int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u);
 int s2s_batched(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, double* Tdev);
+int s2s_check(fit_plan* p);
 void s2s_free(fit_plan* p);
 int triad_m2m(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, int fp64, double* S, double* net);
 }  // namespace fit

@@ -16,10 +16,10 @@ namespace fit {
 
 int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
                   const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
-                  const float2* tw, cudaStream_t st);
+                  const float2* tw, int* err, cudaStream_t st);
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
                   const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
-                  const float2* tw, cudaStream_t st);
+                  const float2* tw, int* err, cudaStream_t st);
 
 struct S2SState {
   cudaGraphExec_t exec = nullptr;
@@ -35,7 +35,7 @@ struct S2SState {
   std::vector<int> occ;   // retained modes per shell
   fit_dbuf occ_dev;
   // fused-path buffers
-  fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart;
+  fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr;
   int fkd_n = -1;
 };
 
@@ -43,7 +43,7 @@ void s2s_free(fit_plan* p) {
   S2SState* s = (S2SState*)p->s2s;
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
-  fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse, &s->fsb, &s->fkd, &s->fA, &s->fB, &s->fpart};
+  fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse, &s->fsb, &s->fkd, &s->fA, &s->fB, &s->fpart, &s->ferr};
   for (fit_dbuf* b : bufs)
     if (b->p) cudaFree(b->p);
   delete s;
@@ -237,6 +237,10 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA * B)));
   FIT_TRY(ensure(p, &s->fB, (size_t)(8.0 * perB * B)));
   FIT_TRY(ensure(p, &s->fpart, sizeof(double) * (size_t)B * npt * nsh));
+  if (!s->ferr.p) {   // wait-timeout flag of the bulk-copy kernels (allocated and cleared once, outside capture)
+    FIT_TRY(ensure(p, &s->ferr, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(s->ferr.p, 0, sizeof(int)));
+  }
   FIT_TRY(ensure(p, &p->hs, sizeof(float2) * 3 * g.Mhalf));
   FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
   if (s->fkd_n != KY) {   // derivative multipliers of the live indices (never during capture)
@@ -295,10 +299,10 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
     for (int b = 0; b < a.nb; ++b) a.med[b] = meds[b0 + b];
     int rc = fz_dispatch_a(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
-                           (float2*)s->fB.p, (double*)s->fpart.p, tw, p->stream);
+                           (float2*)s->fB.p, (double*)s->fpart.p, tw, (int*)s->ferr.p, p->stream);
     if (rc == 1)
       rc = fz_dispatch_b(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
-                         (float2*)s->fB.p, (double*)s->fpart.p, tw, p->stream);
+                         (float2*)s->fB.p, (double*)s->fpart.p, tw, (int*)s->ferr.p, p->stream);
     if (rc != FIT_OK) {
       if (rc == 1) fit_set_error("no fused kernels for size %d", M);
       return rc == 1 ? FIT_ERR_SIZE : rc;
@@ -313,6 +317,21 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
 static int run_s2s(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {
   if (fused_ok(p)) return run_fused(p, s, ud, ad, inv, Td);
   return (p->prec == 64) ? run_batched<double>(p, s, ud, ad, inv, Td) : run_batched<float>(p, s, ud, ad, inv, Td);
+}
+
+// A bounded wait inside a bulk-copy kernel that gave up leaves its flag set: report it.
+int s2s_check(fit_plan* p) {
+  S2SState* s = (S2SState*)p->s2s;
+  if (!s || !s->ferr.p) return FIT_OK;
+  int h = 0;
+  FIT_CUDA_CHECK(cudaMemcpyAsync(&h, s->ferr.p, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));
+  if (h) {
+    FIT_CUDA_CHECK(cudaMemset(s->ferr.p, 0, sizeof(int)));
+    fit_set_error("a bulk-copy wait timed out inside the fused shell-to-shell kernels");
+    return FIT_ERR_STATE;
+  }
+  return FIT_OK;
 }
 
 int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td) {
