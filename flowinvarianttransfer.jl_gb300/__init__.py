@@ -2,7 +2,8 @@
 
 Python host mirror of the reference API over libfit_gb300.so (hand-written CUDA for sm_103a):
 the pseudospectral nonlinear term with 2/3 or 3/2 dealiasing and the shell-binned reductions
-built on it — spectral flux, shell-to-shell, partial fluxes, mode-to-mode.
+built on it — spectral flux, shell-to-shell, partial fluxes, mode-to-mode — plus the
+coarse-graining flux, a forced Navier-Stokes evolver and the learned subfilter-stress closure.
 """
 from .types import *  # noqa: F401,F403
 from .shells import (wavenumber_grid, shell_edges, shell_centers, n_shells, default_binning, kmax,  # noqa: F401
@@ -13,5 +14,8 @@ from .api import (compute_nonlinear_term, transfer_density, decompose_field, ass
                   calculate_helical_partial_fluxes, calculate_mode_to_mode_transfer,
                   calculate_scalar_mode_to_mode_transfer, calculate_energy_transfer)
 from .plan import Plan, get_plan, clear_plans  # noqa: F401
+from .closure import (calculate_coarse_graining_flux, evolve_forced_navier_stokes,  # noqa: F401
+                      evolve_forced_navier_stokes_device, closure_data, ClosureData, SubfilterStressMLP,
+                      gradient_model_flux, field_compare)
 from . import _lib  # noqa: F401
 from ._lib import FitError, launch_count, lib_path  # noqa: F401

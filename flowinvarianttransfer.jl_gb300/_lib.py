@@ -14,6 +14,8 @@ EXPORTS = [
     "fit_launch_count", "fit_nonlinear_term", "fit_assign_shells", "fit_transfer_density",
     "fit_spectral_flux", "fit_shell_to_shell", "fit_helical_decompose", "fit_helmholtz_decompose",
     "fit_partial_fluxes", "fit_mode_to_mode", "fit_prof_enable", "fit_prof_read", "fit_prof_kind_name",
+    "fit_coarse_graining_flux", "fit_forward_spectrum", "fit_ns_evolve", "fit_mlp_nparams", "fit_mlp_forward",
+    "fit_mlp_train_grad", "fit_mlp_adam", "fit_gradient_model_flux", "fit_field_moments", "fit_field_compare",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -51,6 +53,17 @@ def _declare(lib):
     lib.fit_prof_read.argtypes = [i32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     lib.fit_prof_kind_name.restype = C.c_char_p
     lib.fit_prof_kind_name.argtypes = [i32]
+    f32 = C.c_float
+    lib.fit_coarse_graining_flux.argtypes = [vp, vp, C.c_double, i32, vp, vp, vp, dp, i32]
+    lib.fit_forward_spectrum.argtypes = [vp, vp, vp, i32]
+    lib.fit_ns_evolve.argtypes = [vp, vp, i32, C.c_double, C.c_double, C.c_double, C.c_double, i32]
+    lib.fit_mlp_nparams.argtypes = []
+    lib.fit_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp, vp, vp, vp]
+    lib.fit_mlp_train_grad.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, vp, vp, vp]
+    lib.fit_gradient_model_flux.argtypes = [vp, i64, i64, C.c_double, vp, vp, vp]
+    lib.fit_field_moments.argtypes = [vp, i64, i64, i32, vp, vp]
+    lib.fit_field_compare.argtypes = [vp, vp, i64, vp, vp]
+    lib.fit_mlp_adam.argtypes = [vp, vp, vp, vp, i32, f32, f32, f32, f32, vp]
     for name in EXPORTS:
         if name not in ("fit_last_error", "fit_launch_count", "fit_prof_kind_name"):
             getattr(lib, name).restype = C.c_int

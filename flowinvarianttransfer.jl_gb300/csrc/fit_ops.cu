@@ -42,6 +42,16 @@ __global__ void k_gather(GridDesc g, KTab kt, GatherArgs a, V* out) {
     if (f.band > 0 && a.shell_full[k.lin] != f.band) continue;
     double2 v = ld_c(a.src[f.src], a.in_f64, k.lin + a.src_comp_stride[f.src] * f.comp);
     if (f.deriv >= 0) v = dmul_i(v, kt.k[f.deriv][k.k[f.deriv]]);
+    if (f.filt) {
+      double k2 = 0.0;
+      for (int d = 0; d < g.nd; ++d) {
+        const double kd = kt.k[d][k.k[d]];
+        k2 += kd * kd;
+      }
+      const double G = filter_response(a.filter_kind, sqrt(k2), a.ell);
+      v.x *= G;
+      v.y *= G;
+    }
     if (s == 1) v.y = -v.y;
     acc.x += v.x;
     acc.y += v.y;

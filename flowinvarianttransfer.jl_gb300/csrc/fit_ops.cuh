@@ -55,6 +55,7 @@ struct GatherField {
   int comp;    // component of the source
   int deriv;   // derivative axis or -1
   int band;    // 1-based shell restriction, 0 = none
+  int filt;    // 1: multiply by the filter response G(|k|, ell) of GatherArgs
 };
 struct GatherArgs {
   const void* src[2];
@@ -65,7 +66,20 @@ struct GatherArgs {
   int nfields;
   GatherField f[16];
   double scale;
+  int filter_kind;   // 0 sharp, 1 Gaussian, 2 top-hat (src/Filters.jl:19-26)
+  double ell;        // filter scale
 };
+
+// Spectral filter response G(k, ell) (src/Filters.jl:19-26): sharp 1[|k| < pi/ell], Gaussian
+// exp(-k^2 ell^2 / 24), top-hat sinc(k ell / (2 pi)) with the normalised sinc.
+__device__ __forceinline__ double filter_response(int kind, double k, double ell) {
+  const double PI = 3.14159265358979323846;
+  if (kind == 0) return fabs(k) < PI / ell ? 1.0 : 0.0;
+  if (kind == 1) return exp(-k * k * ell * ell / 24.0);
+  const double x = k * ell / (2.0 * PI);
+  if (x == 0.0) return 1.0;
+  return sin(PI * x) / (PI * x);
+}
 template <typename T>
 int gather_half(const GridDesc& g, const KTab& kt, const GatherArgs& a, typename Vec2<T>::t* out, cudaStream_t st);
 

@@ -159,6 +159,40 @@ class Plan:
                                             self._vp(net), PTR_HOST))
         return S, net
 
+    def forward_spectrum(self, u_phys):
+        """û = fft(u)/Np of real physical fields (ns..., M) computed on the device."""
+        rdt = np.float64 if self.io_f64 else np.float32
+        u = np.asarray(u_phys)
+        if u.ndim == self.nd:
+            u = u[..., None]
+        if u.shape != self.ns + (self.M,):
+            raise ValueError(f"field has shape {u.shape}; expected {self.ns + (self.M,)}")
+        u = np.asfortranarray(u.astype(rdt, copy=False))
+        out = np.empty(self.ns + (self.M,), dtype=self.cdtype, order="F")
+        with self.lock:
+            check(self.lib.fit_forward_spectrum(self.h, self._vp(u), self._vp(out), PTR_HOST))
+        return out
+
+    def coarse_graining_flux(self, u_hat, ell, filter_code, diagnostics=False):
+        u = self._field(u_hat, self.M)
+        rdt = np.float64 if self.precision == 64 else np.float32
+        nd = self.nd
+        Pi = np.empty(self.ns, dtype=rdt, order="F")
+        A = np.empty(self.ns + (nd * nd,), dtype=rdt, order="F") if diagnostics else None
+        tau = np.empty(self.ns + (nd * (nd + 1) // 2,), dtype=rdt, order="F") if diagnostics else None
+        mean = C.c_double()
+        with self.lock:
+            check(self.lib.fit_coarse_graining_flux(self.h, self._vp(u), float(ell), int(filter_code), self._vp(Pi),
+                                                    self._vp(A), self._vp(tau), C.byref(mean), PTR_HOST))
+        return Pi, float(mean.value), A, tau
+
+    def ns_evolve(self, u_hat, nsteps, dt, nu, kf, power):
+        u = np.array(self._field(u_hat, self.M), order="F", copy=True)
+        with self.lock:
+            check(self.lib.fit_ns_evolve(self.h, self._vp(u), int(nsteps), float(dt), float(nu), float(kf),
+                                         float(power), PTR_HOST))
+        return u
+
     # ---- device-pointer entry points (inputs already resident in HBM) ----
     def shell_to_shell_device(self, u_ptr, a_ptr, edges, dmask, coord_f32, inv, mode, T_ptr, net_ptr, asym_ptr,
                               verify=True):
@@ -167,6 +201,22 @@ class Plan:
                                           len(e), dmask, int(coord_f32), inv, mode, int(verify), C.c_void_p(T_ptr),
                                           C.c_void_p(net_ptr) if net_ptr else None,
                                           C.c_void_p(asym_ptr) if asym_ptr else None, PTR_DEVICE))
+
+
+    def coarse_graining_flux_device(self, u_ptr, ell, filter_code, Pi_ptr, A_ptr=0, tau_ptr=0):
+        mean = C.c_double()
+        check(self.lib.fit_coarse_graining_flux(self.h, C.c_void_p(u_ptr), float(ell), int(filter_code),
+                                                C.c_void_p(Pi_ptr), C.c_void_p(A_ptr) if A_ptr else None,
+                                                C.c_void_p(tau_ptr) if tau_ptr else None, C.byref(mean),
+                                                PTR_DEVICE))
+        return float(mean.value)
+
+    def ns_evolve_device(self, u_ptr, nsteps, dt, nu, kf, power):
+        check(self.lib.fit_ns_evolve(self.h, C.c_void_p(u_ptr), int(nsteps), float(dt), float(nu), float(kf),
+                                     float(power), PTR_DEVICE))
+
+    def forward_spectrum_device(self, u_ptr, out_ptr):
+        check(self.lib.fit_forward_spectrum(self.h, C.c_void_p(u_ptr), C.c_void_p(out_ptr), PTR_DEVICE))
 
 
 _CACHE: "OrderedDict[tuple, Plan]" = OrderedDict()

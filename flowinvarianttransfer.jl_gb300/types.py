@@ -125,6 +125,23 @@ class DivergentDecomposition(AbstractFieldDecomposition):
     pass
 
 
+# ---- filters (src/Types.jl filter types, src/Filters.jl:19-26) ----------------------------------
+class AbstractFilter:
+    code = -1
+
+
+class SharpSpectralFilter(AbstractFilter):
+    code = 0
+
+
+class GaussianFilter(AbstractFilter):
+    code = 1
+
+
+class TopHatFilter(AbstractFilter):
+    code = 2
+
+
 # ---- backends -----------------------------------------------------------------------------------
 class AbstractSpectralBackend:
     pass
@@ -211,3 +228,22 @@ class PartialFluxResult:
     channels: dict
     total: SpectralFluxResult
     k_shells: np.ndarray
+
+
+@dataclass
+class CoarseGrainingFluxResult:
+    """src/Types.jl:673-677."""
+    filter_scale: float
+    flux_field: np.ndarray
+    mean_flux: float
+
+
+@dataclass
+class CoarseGrainingFluxResultWithDiagnostics:
+    """src/Types.jl:681-: the flux plus the subfilter stress tau_ij and filtered strain S_ij,
+    each of shape (ns..., nd, nd)."""
+    filter_scale: float
+    flux_field: np.ndarray
+    mean_flux: float
+    tau: np.ndarray
+    strain: np.ndarray

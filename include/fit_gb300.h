@@ -131,6 +131,62 @@ int fit_partial_fluxes(fit_plan* plan, const void* u_hat, int decomposition, int
 int fit_mode_to_mode(fit_plan* plan, const void* u_hat, const void* adv_hat, int invariant, int fp64_products,
                      double* S, double* net, int ptr_kind);
 
+/* Coarse-graining energy flux Pi_ell(x) = -tau_ij S_ij of the physical velocity u = sum_k û e^{ikx}
+ * (û = fft(u)/Np), filter_kind 0 sharp / 1 Gaussian / 2 top-hat at scale ell (src/Filters.jl:19-26).
+ * Restates calculate_coarse_graining_flux (src/CoarseGrainingFlux.jl:60-72), which the reference
+ * delegates to the 2D-only CoarseGrainingEnergyFluxes.jl, for 2D and 3D. Pi is written in the plan
+ * precision (N^D points, x fastest); A_out (nd*nd fields of d_j ū_i, component i*nd+j) and tau_out
+ * (nd(nd+1)/2 fields, order 00 11 22 01 02 12) are optional outputs in the plan precision;
+ * Pi_mean is the mean. u_hat uses the package convention û = fft(u)/Np. */
+int fit_coarse_graining_flux(fit_plan* plan, const void* u_hat, double ell, int filter_kind, void* Pi,
+                             void* A_out, void* tau_out, double* Pi_mean, int ptr_kind);
+
+/* û = fft(u)/Np (the package coefficient convention, src/FlowInvariantTransfer.jl:242) of the
+ * plan's n_advected real physical fields (x fastest, io element type), written as the full N-grid
+ * spectrum. Replaces the host FFTW.fft a caller of the reference runs before every spectral call;
+ * unpadded plans only. */
+int fit_forward_spectrum(fit_plan* plan, const void* u_phys, void* u_hat, int ptr_kind);
+
+/* Advances û in place by nsteps of SSP-RK3 for forced incompressible Navier-Stokes,
+ * dû/dt = -P[N̂(û)] - nu k^2 û + alpha û 1[0 < |k| <= kf], alpha = power / (2 E_f), with this
+ * library's nonlinear term (the plan's dealiasing). The reference's examples/flows.jl:28-89
+ * evolver is unforced RK2; this forced RK3 form has no reference counterpart. */
+int fit_ns_evolve(fit_plan* plan, void* u_hat, int nsteps, double dt, double nu, double kf, double power,
+                  int ptr_kind);
+
+/* ---- learned subfilter-stress closure (no counterpart in the reference) -------------------------
+ * A pointwise MLP 9 -> 64 -> 64 -> 6 (ReLU) maps the filtered velocity-gradient tensor A_ij = d_j ū_i
+ * (9 features) to the six subfilter-stress components (tau_00 tau_11 tau_22 tau_01 tau_02 tau_12).
+ * Tensor-core kernels: BF16 operands (weights, features, activations), FP32 accumulation. params is
+ * the FP32 master copy (fit_mlp_nparams() floats: W1[64][16], b1[64], W2[64][64], b2[64], W3[8][64],
+ * b3[8]; input columns 9..15 and output rows 6..7 are padding that stays zero). Point data is
+ * field-major: X[9][P], T/Y[6][P]. Features are multiplied by in_scale[9] and targets by t_scale[6]
+ * before the network sees them; fit_mlp_forward divides its outputs by t_scale again. All pointers
+ * are device pointers; stream may be NULL. */
+int fit_mlp_nparams(void);
+/* Y (6 x ld, optional) = predicted stress; Pi (P, optional) = -tau_ij S_ij of the prediction with
+ * S = (A + A^T)/2 taken from the unscaled features (the closure's flux, fused). */
+int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
+                    const float* t_scale, float* Y, float* Pi, void* stream);
+/* Adds to grad (not cleared) the gradient of loss = sum_p sum_o (Y_po - t_scale_o T_op)^2 / Ptot over
+ * the P points given (Ptot: points of the whole minibatch, for split calls), and to *loss the sum of
+ * squared scaled errors. */
+int fit_mlp_train_grad(const float* params, const float* X, const float* T, int64_t ld, int64_t P, int64_t Ptot,
+                       const float* in_scale, const float* t_scale, float* grad, double* loss, void* stream);
+/* One Adam step (bias-corrected, step >= 1) on params with moment buffers m, v. */
+int fit_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
+                 float beta2, float eps, void* stream);
+
+/* Gradient (Clark) model baseline for a Gaussian filter, tau_ij = ell^2/12 A_ik A_jk, on the same
+ * field-major A (9 x ld): tau (6 x ld) and/or Pi = -tau_ij S_ij (P), each optional. */
+int fit_gradient_model_flux(const float* A, int64_t ld, int64_t P, double ell, float* tau, float* Pi,
+                            void* stream);
+/* FP64 reductions for normalisation and scoring, device outputs: fit_field_moments writes
+ * (sum x, sum x^2) per field (2*nf doubles); fit_field_compare writes (sum a, sum b, sum a^2,
+ * sum b^2, sum ab, sum (a-b)^2). */
+int fit_field_moments(const float* X, int64_t ld, int64_t P, int nf, double* out, void* stream);
+int fit_field_compare(const float* a, const float* b, int64_t P, double* out, void* stream);
+
 /* Allocation-free variant of fit_mode_to_mode, for callers that cannot allocate device memory
  * (a caller-owned memory budget or allocator, a latency-critical loop where an allocation would
  * synchronise the device, an embedding runtime that only lends its own buffers). It has no
