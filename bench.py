@@ -49,6 +49,14 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="s2s", choices=["s2s", "closure"],
+                    help="s2s: the 512^3 shell-to-shell headline; closure: learned closure vs exact "
+                         "coarse-graining flux on a forced 256^3 field")
+    ap.add_argument("--closure-n", type=int, default=256)
+    ap.add_argument("--closure-nsteps", type=int, default=200)
+    ap.add_argument("--train-steps", type=int, default=1500)
+    ap.add_argument("--train-batch", type=int, default=65536)
+    ap.add_argument("--lr", type=float, default=2e-3)
     return ap.parse_args()
 
 
@@ -81,9 +89,10 @@ def allmax(ws, x):
     return float(t.item())
 
 
-def make_field(N, seed, device):
-    """û = fft(u)/Np of real Gaussian noise per component, scaled by sqrt(E(|k|)/|k|^2) with
-    E = k^-5/3 on [4, 170], (k/4)^4 4^-5/3 below 4, 0 above; Leray-projected, mean removed.
+def make_field(N, seed, device, spectrum="kolmogorov"):
+    """û = fft(u)/Np of real Gaussian noise per component, scaled by sqrt(E(|k|)/|k|^2), with
+    E = k^-5/3 on [4, 170], (k/4)^4 4^-5/3 below 4, 0 above ("kolmogorov") or
+    E = k^4 exp(-2 (k/8)^2) ("k4exp8"); Leray-projected, mean removed.
     Returned as a (3, N, N, N) complex64 CUDA tensor, i.e. the column-major (N, N, N, 3) layout."""
     import torch
     g = torch.Generator(device=device)
@@ -92,8 +101,11 @@ def make_field(N, seed, device):
     kz, ky, kx = k1.view(N, 1, 1), k1.view(1, N, 1), k1.view(1, 1, N)
     k2 = kx * kx + ky * ky + kz * kz
     km = torch.sqrt(k2)
-    E = torch.where(km < 4, (km / 4) ** 4 * 4.0 ** (-5 / 3),
-                    torch.where(km <= 170, km.clamp_min(1e-30) ** (-5 / 3), torch.zeros_like(km)))
+    if spectrum == "k4exp8":
+        E = km ** 4 * torch.exp(-2 * (km / 8) ** 2)
+    else:
+        E = torch.where(km < 4, (km / 4) ** 4 * 4.0 ** (-5 / 3),
+                        torch.where(km <= 170, km.clamp_min(1e-30) ** (-5 / 3), torch.zeros_like(km)))
     amp = torch.where(k2 > 0, torch.sqrt(E / k2.clamp_min(1e-30)), torch.zeros_like(km))
     del E, km
     u = torch.empty((3, N, N, N), dtype=torch.complex64, device=device)
@@ -417,10 +429,94 @@ def run_ours(args):
     return 0
 
 
+def run_closure(args):
+    """Learned closure vs exact coarse-graining flux: a seeded k^4 exp(-2(k/8)^2) field at N^3 is
+    evolved by SSP-RK3 forced Navier-Stokes on the GPU (nu = 2e-3, forcing of 0 < |k| <= 2 at
+    constant power 0.1, dt = 5e-3); for each Gaussian filter k_c in {8, 16, 32} (ell = pi/k_c) the
+    exact path gives A = grad ū, tau and Pi_ell; the MLP trains on the half z < N/2 and is scored on
+    the other half against Pi_ell, beside the gradient (Clark) model and no closure."""
+    import torch
+    import __graft_entry__
+    F = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    N = args.closure_n
+    ns = (N, N, N)
+    ks = F.wavenumber_grid(ns, (2 * np.pi,) * 3)
+    u = make_field(N, args.seed, dev, spectrum="k4exp8")
+    u *= math.sqrt(0.5 / (0.5 * float((u.abs() ** 2).sum())))
+    nu, dt, kf, power = 2e-3, 5e-3, 2.0, 0.1
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    F.evolve_forced_navier_stokes_device(u, ks, 1, dt, nu, kf, power)    # workspace + first step
+    l0 = F.launch_count()
+    e0.record()
+    F.evolve_forced_navier_stokes_device(u, ks, args.closure_nsteps - 1, dt, nu, kf, power)
+    e1.record()
+    torch.cuda.synchronize()
+    evolve_ms = e0.elapsed_time(e1) / max(1, args.closure_nsteps - 1)
+    evolve_launches = (F.launch_count() - l0) / max(1, args.closure_nsteps - 1)
+    energy = 0.5 * float((u.abs() ** 2).sum())
+    n = N ** 3
+    half = n // 2
+    flop_pt = 2 * (9 * 64 + 64 * 64 + 64 * 6)
+    results = {}
+    for kc in (8, 16, 32):
+        ell = math.pi / kc
+        F.closure_data(u, ks, ell)                     # warm the coarse-graining plan
+        torch.cuda.synchronize()
+        e0.record()
+        d = F.closure_data(u, ks, ell)
+        e1.record()
+        torch.cuda.synchronize()
+        exact_ms = e0.elapsed_time(e1)
+        m = F.SubfilterStressMLP(seed=args.seed)
+        t0 = time.perf_counter()
+        hist = m.train(d, 0, half, steps=args.train_steps, batch=args.train_batch, lr=args.lr,
+                       log_every=max(1, args.train_steps // 5))
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+        ev = m.evaluate(d, half, n)
+        for _ in range(3):
+            m.predict(d.A, n, n, want_tau=False)
+        torch.cuda.synchronize()
+        reps = 10
+        e0.record()
+        for _ in range(reps):
+            m.predict(d.A, n, n, want_tau=False)
+        e1.record()
+        torch.cuda.synchronize()
+        inf_ms = e0.elapsed_time(e1) / reps
+        results[str(kc)] = {"ell": ell, "exact_path_ms": exact_ms, "exact_points_per_s": n / (exact_ms / 1e3),
+                            "train_s": train_s, "train_steps": args.train_steps, "train_points_per_step": args.train_batch,
+                            "loss_history": hist, "inference_ms": inf_ms,
+                            "inference_points_per_s": n / (inf_ms / 1e3),
+                            "inference_tflops": n * flop_pt / (inf_ms / 1e3) / 1e12,
+                            "mean_flux_exact": d.mean_flux, **ev}
+        del d, m
+        torch.cuda.empty_cache()
+    headline = results["16"]
+    line = {"metric": "learned closure: inference points/s, Pi_ell correlation and rel L2 vs exact coarse-graining "
+                      "flux (256^3 forced NS, Gaussian k_c = 16)",
+            "value": headline["inference_points_per_s"], "unit": "points/s", "n_gpus": 1, "steps": 10,
+            "warmup": 3, "ms_per_step": headline["inference_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (FP32 accumulation)", "data": "synthetic",
+            "config": {"workload": f"{N}^3 D=3 forced SSP-RK3 NS ({args.closure_nsteps} steps, nu={nu}, dt={dt}, "
+                                   f"forcing 0<|k|<={kf} at power {power}) from k^4 exp(-2(k/8)^2); Gaussian filter "
+                                   "k_c in {8,16,32}, ell = pi/k_c; MLP 9-64-64-6 trained on z < N/2, scored on z >= N/2",
+                       "seed": args.seed},
+            "evolve": {"ms_per_rk3_step": evolve_ms, "launches_per_step": evolve_launches, "energy": energy},
+            "flop_per_point": flop_pt, "results": results}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "closure":
+        return run_closure(args)
     return run_ours(args)
 
 

@@ -58,8 +58,8 @@ def _declare(lib):
     lib.fit_forward_spectrum.argtypes = [vp, vp, vp, i32]
     lib.fit_ns_evolve.argtypes = [vp, vp, i32, C.c_double, C.c_double, C.c_double, C.c_double, i32]
     lib.fit_mlp_nparams.argtypes = []
-    lib.fit_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp, vp, vp, vp]
-    lib.fit_mlp_train_grad.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, vp, vp, vp]
+    lib.fit_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp, i32, vp, vp, vp]
+    lib.fit_mlp_train_grad.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, i32, vp, vp, vp]
     lib.fit_gradient_model_flux.argtypes = [vp, i64, i64, C.c_double, vp, vp, vp]
     lib.fit_field_moments.argtypes = [vp, i64, i64, i32, vp, vp]
     lib.fit_field_compare.argtypes = [vp, vp, i64, vp, vp]

@@ -218,9 +218,13 @@ def init_params(seed=0):
 
 
 class SubfilterStressMLP:
-    """A_ij (9) -> 64 -> 64 -> tau (6), ReLU; BF16 tensor-core kernels with FP32 accumulation."""
+    """A_ij (9) -> 64 -> 64 -> tau (6), ReLU; BF16 tensor-core kernels with FP32 accumulation.
 
-    def __init__(self, seed=0, device=None, params=None):
+    ``homogeneous`` (default): the network sees the direction v/|v| of the scaled gradient tensor
+    and its output is multiplied by s = |v|^2, so the predicted stress is homogeneous of degree 2
+    in A, as the exact subfilter stress is at leading order in ell."""
+
+    def __init__(self, seed=0, device=None, params=None, homogeneous=True):
         torch = _torch()
         self.lib = _lib.load()
         self.nparam = int(self.lib.fit_mlp_nparams())
@@ -237,6 +241,7 @@ class SubfilterStressMLP:
         self.t_scale = torch.ones(6, dtype=torch.float32, device=dev)
         self.step = 0
         self.device = dev
+        self.homogeneous = bool(homogeneous)
 
     # scales: unit variance of every feature and target over the training points
     def fit_scales(self, X, T, ld, P):
@@ -250,15 +255,17 @@ class SubfilterStressMLP:
         sx = (mx[:, 1] / P - (mx[:, 0] / P) ** 2).clamp_min(1e-30).sqrt()
         st = (mt[:, 1] / P).clamp_min(1e-30).sqrt()   # targets are not centred: the bias learns the mean
         self.in_scale.copy_((1.0 / sx).float())
-        self.t_scale.copy_((1.0 / st).float())
+        # homogeneous form: outputs are multiplied by s = |v|^2, whose mean is sum_f E[x_f^2] / var_f
+        gain = float((mx[:, 1] / P / sx ** 2).sum()) if self.homogeneous else 1.0
+        self.t_scale.copy_((gain / st).float())
 
     def grad_of(self, X, T, ld, P, Ptot=None):
         """Gradient of the scaled MSE over points [0, P) of field-major X/T (stride ld)."""
         self.grad.zero_()
         self.loss.zero_()
         check(self.lib.fit_mlp_train_grad(_vp(self.params), _vp(X), _vp(T), ld, P, P if Ptot is None else Ptot,
-                                          _vp(self.in_scale), _vp(self.t_scale), _vp(self.grad), _vp(self.loss),
-                                          _stream()))
+                                          _vp(self.in_scale), _vp(self.t_scale), int(self.homogeneous),
+                                          _vp(self.grad), _vp(self.loss), _stream()))
         return self.grad, self.loss
 
     def train(self, data: ClosureData, p0, p1, steps=1500, batch=65536, lr=2e-3, seed=0, log_every=0):
@@ -287,7 +294,7 @@ class SubfilterStressMLP:
         Y = torch.empty((6, ld), dtype=torch.float32, device=self.device) if want_tau else None
         Pi = torch.empty(P, dtype=torch.float32, device=self.device) if want_flux else None
         check(self.lib.fit_mlp_forward(_vp(self.params), _vp(X), ld, P, _vp(self.in_scale), _vp(self.t_scale),
-                                       _vp(Y), _vp(Pi), _stream()))
+                                       int(self.homogeneous), _vp(Y), _vp(Pi), _stream()))
         return (Y[:, :P] if Y is not None else None), Pi
 
     def evaluate(self, data: ClosureData, p0, p1):

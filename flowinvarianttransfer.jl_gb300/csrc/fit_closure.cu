@@ -130,6 +130,14 @@ static int cg_run(fit_plan* p, const void* ud, double ell, int kind, void* Pi, v
   for (int i = 0; i < nd; ++i) a.f[i] = GatherField{0, i, -1, 0, 0};
   FIT_TRY(gather_half<T>(g, p->kt, a, hs, p->stream));
   FIT_TRY(inverse_nd<T>(hs, u, g, p->ax, nd, (T)1, p->stream));
+  // Filter and differentiate the spectrum of the real field u (Hermitian by construction), so that
+  // an input that is not Hermitian on the Nyquist planes (a Leray split with +N/2 there) gives the
+  // flux of the real velocity it stands for.
+  FIT_TRY(ensure(p, &p->out_c2, sizeof(V) * nd * g.Ntot));
+  FIT_TRY(forward_nd<T>(u, (V*)p->nh.p, g, p->ax, nd, (T)(1.0 / (double)n), p->stream));
+  FIT_TRY(scatter_full<T>(g, (const V*)p->nh.p, nd, 0, p->out_c2.p, sizeof(T) == 8, p->stream));
+  a.src[0] = p->out_c2.p;
+  a.in_f64 = sizeof(T) == 8;
   for (int i = 0; i < nd; ++i) a.f[i] = GatherField{0, i, -1, 0, 1};
   FIT_TRY(gather_half<T>(g, p->kt, a, hs, p->stream));
   FIT_TRY(inverse_nd<T>(hs, ub, g, p->ax, nd, (T)1, p->stream));

@@ -128,9 +128,13 @@ FIT_D void mlp_tile_forward(const MlpSmem* w, const uint32_t* xa, uint32_t h1a[4
   }
 }
 
-// A fragment of 16 points x 16 features (9 real) from field-major X, scaled, BF16.
+// A fragment of 16 points x 16 features (9 real) from field-major X, scaled, BF16. In the
+// homogeneous form the scaled features v are divided by |v| (s = |v|^2 returned per row g / g+8):
+// the network sees the direction of the gradient tensor and its output is multiplied by s, so the
+// predicted stress is homogeneous of degree 2 in A, like the exact subfilter stress at leading
+// order (tau ~ ell^2/12 A A^T for a Gaussian filter).
 FIT_D void mlp_load_x(const float* __restrict__ X, long ld, long P, long p0, const float* sc, uint32_t* xa,
-                      int lane) {
+                      int lane, bool homog, float* s) {
   const int g = lane >> 2, t = lane & 3;
   float v[2][2][2];   // [row g / g+8][col group 2t / 2t+8][pair]
 #pragma unroll
@@ -143,6 +147,20 @@ FIT_D void mlp_load_x(const float* __restrict__ X, long ld, long P, long p0, con
         const long p = p0 + g + 8 * r;
         v[r][cg][e] = (f < 9 && p < P) ? X[(long)f * ld + p] * sc[f] : 0.f;
       }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    float q = v[r][0][0] * v[r][0][0] + v[r][0][1] * v[r][0][1] + v[r][1][0] * v[r][1][0] + v[r][1][1] * v[r][1][1];
+    q += __shfl_xor_sync(0xffffffffu, q, 1);   // the quad of lanes holding row g (g+8)
+    q += __shfl_xor_sync(0xffffffffu, q, 2);
+    s[r] = homog ? q : 1.f;
+    if (homog) {
+      const float inv = q > 0.f ? 1.f / sqrtf(q) : 0.f;
+#pragma unroll
+      for (int cg = 0; cg < 2; ++cg)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) v[r][cg][e] *= inv;
+    }
+  }
   xa[0] = pack_bf16(v[0][0][0], v[0][0][1]);
   xa[1] = pack_bf16(v[1][0][0], v[1][0][1]);
   xa[2] = pack_bf16(v[0][1][0], v[0][1][1]);
@@ -159,7 +177,7 @@ FIT_D float stress_dot_strain(int o, float tau, const float* __restrict__ X, lon
 __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ Pm, const float* __restrict__ X,
                                                      long ld, long P, const float* __restrict__ in_scale,
                                                      const float* __restrict__ t_scale, float* __restrict__ Y,
-                                                     float* __restrict__ Pi) {
+                                                     float* __restrict__ Pi, int homog) {
   __shared__ MlpSmem w;
   __shared__ float sc[9], osc[6];
   mlp_load_weights(&w, Pm, threadIdx.x, blockDim.x);
@@ -172,8 +190,8 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ P
   for (long tile = (long)blockIdx.x * nw + warp; tile < ntile; tile += (long)gridDim.x * nw) {
     const long p0 = tile * 16;
     uint32_t xa[4], h1a[4][4], h2a[4][4];
-    float y[4];
-    mlp_load_x(X, ld, P, p0, sc, xa, lane);
+    float y[4], sn[2];
+    mlp_load_x(X, ld, P, p0, sc, xa, lane, homog != 0, sn);
     mlp_tile_forward(&w, xa, h1a, h2a, y, lane);
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
@@ -183,7 +201,7 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ P
       for (int e = 0; e < 2; ++e) {
         const int o = 2 * t + e;
         if (o < 6 && p < P) {
-          const float tau = y[2 * r + e] * osc[o];
+          const float tau = y[2 * r + e] * sn[r] * osc[o];
           if (Y) Y[(long)o * ld + p] = tau;
           if (Pi) part += stress_dot_strain(o, tau, X, ld, p);
         }
@@ -243,7 +261,7 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float* __restrict__ Pm,
                                                    const float* __restrict__ T, long ld, long P, long Ptot,
                                                    const float* __restrict__ in_scale,
                                                    const float* __restrict__ t_scale, float* __restrict__ grad,
-                                                   double* __restrict__ loss) {
+                                                   double* __restrict__ loss, int homog) {
   // weights + staged activations exceed the 48 KB static limit: dynamic shared memory
   extern __shared__ __align__(16) unsigned char mlp_dyn_smem[];
   MlpSmem& w = *reinterpret_cast<MlpSmem*>(mlp_dyn_smem);
@@ -273,10 +291,10 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float* __restrict__ Pm,
     const long p0 = blk * 64 + warp * 16;
     const int r0 = warp * 16;
     uint32_t xa[4], h1a[4][4], h2a[4][4];
-    float y[4];
-    mlp_load_x(X, ld, P, p0, sc, xa, lane);
+    float y[4], sn[2];
+    mlp_load_x(X, ld, P, p0, sc, xa, lane, homog != 0, sn);
     mlp_tile_forward(&w, xa, h1a, h2a, y, lane);
-    // dY = 2 (Y - T) / Ptot on the 6 real outputs (scaled units)
+    // dY = 2 (s Y - T) s / Ptot on the 6 real outputs (scaled units; s = 1 unless homogeneous)
     float dy[4];
 #pragma unroll
     for (int r = 0; r < 2; ++r)
@@ -286,9 +304,9 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float* __restrict__ Pm,
         const long p = p0 + g + 8 * r;
         float d = 0.f;
         if (o < 6 && p < P) {
-          const float diff = y[2 * r + e] - T[(long)o * ld + p] * tsc[o];
+          const float diff = y[2 * r + e] * sn[r] - T[(long)o * ld + p] * tsc[o];
           lsum += (double)diff * diff;
-          d = inv * diff;
+          d = inv * diff * sn[r];
         }
         dy[2 * r + e] = d;
       }
@@ -493,7 +511,7 @@ using namespace fit;
 extern "C" int fit_mlp_nparams(void) { return MLP_NPARAM; }
 
 extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
-                               const float* t_scale, float* Y, float* Pi, void* stream) {
+                               const float* t_scale, int homogeneous, float* Y, float* Pi, void* stream) {
   if (!params || !X || !in_scale || !t_scale || (!Y && !Pi) || P < 0 || ld < P) {
     fit_set_error("bad argument (need params, X, scales, one of Y/Pi, 0 <= P <= ld)");
     return FIT_ERR_ARG;
@@ -503,14 +521,14 @@ extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, 
   const long ntile = (P + 15) / 16;
   long blocks = (ntile + 7) / 8;
   if (blocks > 152 * 8) blocks = 152 * 8;
-  k_mlp_forward<<<(unsigned)blocks, 256, 0, st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi);
+  k_mlp_forward<<<(unsigned)blocks, 256, 0, st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi, homogeneous);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
 
 extern "C" int fit_mlp_train_grad(const float* params, const float* X, const float* T, int64_t ld, int64_t P,
-                                  int64_t Ptot, const float* in_scale, const float* t_scale, float* grad,
-                                  double* loss, void* stream) {
+                                  int64_t Ptot, const float* in_scale, const float* t_scale, int homogeneous,
+                                  float* grad, double* loss, void* stream) {
   if (!params || !X || !T || !in_scale || !t_scale || !grad || !loss || P <= 0 || Ptot <= 0 || ld < P) {
     fit_set_error("bad argument");
     return FIT_ERR_ARG;
@@ -526,7 +544,8 @@ extern "C" int fit_mlp_train_grad(const float* params, const float* X, const flo
     FIT_CUDA_CHECK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (dev >= 0 && dev < 64) attr_set[dev] = true;
   }
-  k_mlp_train<<<(unsigned)blocks, 128, smem, st>>>(params, X, T, ld, P, Ptot, in_scale, t_scale, grad, loss);
+  k_mlp_train<<<(unsigned)blocks, 128, smem, st>>>(params, X, T, ld, P, Ptot, in_scale, t_scale, grad, loss,
+                                                    homogeneous);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }

@@ -160,19 +160,22 @@ int fit_ns_evolve(fit_plan* plan, void* u_hat, int nsteps, double dt, double nu,
  * Tensor-core kernels: BF16 operands (weights, features, activations), FP32 accumulation. params is
  * the FP32 master copy (fit_mlp_nparams() floats: W1[64][16], b1[64], W2[64][64], b2[64], W3[8][64],
  * b3[8]; input columns 9..15 and output rows 6..7 are padding that stays zero). Point data is
- * field-major: X[9][P], T/Y[6][P]. Features are multiplied by in_scale[9] and targets by t_scale[6]
- * before the network sees them; fit_mlp_forward divides its outputs by t_scale again. All pointers
- * are device pointers; stream may be NULL. */
+ * field-major with field stride ld >= P: X[9][ld], T/Y[6][ld]. Features are multiplied by
+ * in_scale[9] and targets by t_scale[6] before the network sees them; fit_mlp_forward divides its
+ * outputs by t_scale again. homogeneous != 0: with v the scaled features and s = |v|^2, the network
+ * sees v/|v| and its outputs are multiplied by s (a stress homogeneous of degree 2 in A). All
+ * pointers are device pointers; stream may be NULL. */
 int fit_mlp_nparams(void);
 /* Y (6 x ld, optional) = predicted stress; Pi (P, optional) = -tau_ij S_ij of the prediction with
  * S = (A + A^T)/2 taken from the unscaled features (the closure's flux, fused). */
 int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
-                    const float* t_scale, float* Y, float* Pi, void* stream);
-/* Adds to grad (not cleared) the gradient of loss = sum_p sum_o (Y_po - t_scale_o T_op)^2 / Ptot over
- * the P points given (Ptot: points of the whole minibatch, for split calls), and to *loss the sum of
- * squared scaled errors. */
+                    const float* t_scale, int homogeneous, float* Y, float* Pi, void* stream);
+/* Adds to grad (not cleared) the gradient of loss = sum_p sum_o (s_p y_po - t_scale_o T_op)^2 / Ptot
+ * (y: network output, s_p = 1 unless homogeneous) over the P points given (Ptot: points of the
+ * whole minibatch, for split calls), and to *loss the sum of squared scaled errors. */
 int fit_mlp_train_grad(const float* params, const float* X, const float* T, int64_t ld, int64_t P, int64_t Ptot,
-                       const float* in_scale, const float* t_scale, float* grad, double* loss, void* stream);
+                       const float* in_scale, const float* t_scale, int homogeneous, float* grad, double* loss,
+                       void* stream);
 /* One Adam step (bias-corrected, step >= 1) on params with moment buffers m, v. */
 int fit_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
                  float beta2, float eps, void* stream);

@@ -112,8 +112,9 @@ def _f32(x):
     return np.asarray(x, dtype=np.float32).astype(np.float64)
 
 
-def mlp_forward(params, X, in_scale, t_scale, emulate_bf16=False):
-    """X: (9, P) features; returns (Y (6, P) in target units, cache)."""
+def mlp_forward(params, X, in_scale, t_scale, emulate_bf16=False, homogeneous=False):
+    """X: (9, P) features; returns (Y (6, P) in target units, cache). ``homogeneous``: the network
+    sees v/|v| (v: scaled features) and its output is multiplied by s = |v|^2."""
     d = mlp_unpack(params)
     r = bf16 if emulate_bf16 else (lambda v: v)
     W1, W2, W3 = r(d["W1"]), r(d["W2"]), r(d["W3"])
@@ -121,27 +122,32 @@ def mlp_forward(params, X, in_scale, t_scale, emulate_bf16=False):
     x = np.zeros((P, 16))
     x[:, :9] = (_f32(np.asarray(X, np.float32) * np.asarray(in_scale, np.float32)[:, None]) if emulate_bf16
                 else np.asarray(X, np.float64) * np.asarray(in_scale, np.float64)[:, None]).T
+    s = np.ones(P)
+    if homogeneous:
+        s = np.sum(x * x, axis=1)
+        with np.errstate(divide="ignore"):
+            x = x * np.where(s > 0, 1.0 / np.sqrt(np.where(s > 0, s, 1.0)), 0.0)[:, None]
     x = r(x)
     z1 = x @ W1.T + d["b1"]
     h1 = r(np.maximum(z1, 0))
     z2 = h1 @ W2.T + d["b2"]
     h2 = r(np.maximum(z2, 0))
     y = h2 @ W3.T + d["b3"]
-    Y = (y[:, :6] / np.asarray(t_scale, np.float64)).T
-    return Y, dict(x=x, h1=h1, h2=h2, y=y, W2=W2, W3=W3)
+    Y = (y[:, :6] * s[:, None] / np.asarray(t_scale, np.float64)).T
+    return Y, dict(x=x, h1=h1, h2=h2, y=y, W2=W2, W3=W3, s=s)
 
 
-def mlp_loss_grad(params, X, T, in_scale, t_scale, emulate_bf16=False):
-    """loss = sum_p sum_o (y_po - t_scale_o T_op)^2 / P and its gradient (NPARAM,)."""
-    _, c = mlp_forward(params, X, in_scale, t_scale, emulate_bf16)
+def mlp_loss_grad(params, X, T, in_scale, t_scale, emulate_bf16=False, homogeneous=False):
+    """loss = sum_p sum_o (s_p y_po - t_scale_o T_op)^2 / P and its gradient (NPARAM,)."""
+    _, c = mlp_forward(params, X, in_scale, t_scale, emulate_bf16, homogeneous)
     r = bf16 if emulate_bf16 else (lambda v: v)
     P = X.shape[1]
     tgt = np.zeros((P, 8))
     tgt[:, :6] = (np.asarray(T, np.float64) * np.asarray(t_scale, np.float64)[:, None]).T
-    diff = c["y"] - tgt
+    diff = c["y"] * c["s"][:, None] - tgt
     diff[:, 6:] = 0.0
     loss = float(np.sum(diff ** 2))
-    dy = r(2.0 * diff / P)
+    dy = r(2.0 * diff * c["s"][:, None] / P)
     dh2 = r((dy @ c["W3"]) * (c["h2"] > 0))
     dh1 = r((dh2 @ c["W2"]) * (c["h1"] > 0))
     g = {"W3": dy.T @ c["h2"], "b3": dy.sum(0), "W2": dh2.T @ c["h1"], "b2": dh2.sum(0),

@@ -32,15 +32,16 @@ def test_oracle_mlp_gradient_finite_differences():
     X = rng.standard_normal((9, 37))
     T = rng.standard_normal((6, 37))
     isc, tsc = rng.uniform(0.5, 2, 9), rng.uniform(0.5, 2, 6)
-    _, g = OC.mlp_loss_grad(p, X, T, isc, tsc)
     idx = [0, 5, 8, 64 * 16 - 8 + 1, 1024 + 3, 1088 + 700, 5184 + 63, 5248 + 5 * 64 + 7, 5760 + 5]
-    for i in idx:
-        e = np.zeros_like(p)
-        e[i] = 1e-6
-        lp, _ = OC.mlp_loss_grad(p + e, X, T, isc, tsc)
-        lm, _ = OC.mlp_loss_grad(p - e, X, T, isc, tsc)
-        fd = (lp - lm) / 2e-6 / X.shape[1]
-        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (i, fd, g[i])
+    for homog in (False, True):
+        _, g = OC.mlp_loss_grad(p, X, T, isc, tsc, homogeneous=homog)
+        for i in idx:
+            e = np.zeros_like(p)
+            e[i] = 1e-6
+            lp, _ = OC.mlp_loss_grad(p + e, X, T, isc, tsc, homogeneous=homog)
+            lm, _ = OC.mlp_loss_grad(p - e, X, T, isc, tsc, homogeneous=homog)
+            fd = (lp - lm) / 2e-6 / X.shape[1]
+            assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (homog, i, fd, g[i])
     # the padding (input columns 9..15, output rows 6..7) gets no gradient
     d = OC.mlp_unpack(g)
     assert np.all(d["W1"][:, 9:] == 0) and np.all(d["W3"][6:] == 0) and np.all(d["b3"][6:] == 0)
@@ -240,33 +241,35 @@ def _rel(a, b):
 
 
 @pytest.mark.gpu
-def test_mlp_forward_matches_oracle():
+@pytest.mark.parametrize("homog", [False, True])
+def test_mlp_forward_matches_oracle(homog):
     P, ld = 1000, 1037
     p, X, T, isc, tsc = _mlp_case(P, ld)
-    m = F.SubfilterStressMLP(params=p)
+    m = F.SubfilterStressMLP(params=p, homogeneous=homog)
     m.in_scale.copy_(_dev(isc))
     m.t_scale.copy_(_dev(tsc))
     Y, Pi = m.predict(_dev(X), ld, P)
     Y = Y.cpu().numpy()
     Pi = Pi.cpu().numpy()
-    Ye, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, emulate_bf16=True)
-    Y64, _ = OC.mlp_forward(p, X[:, :P], isc, tsc)
+    Ye, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, emulate_bf16=True, homogeneous=homog)
+    Y64, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, homogeneous=homog)
     assert _rel(Y, Ye) <= 2e-3           # same BF16 rounding points, FP32 vs FP64 accumulation
     assert _rel(Y, Y64) <= 3e-2          # BF16 quantisation of weights, features and activations
     assert _rel(Pi, OC.flux_from_stress(Y.astype(np.float64), X[:, :P].astype(np.float64))) <= 1e-5
 
 
 @pytest.mark.gpu
-def test_mlp_gradient_matches_oracle():
+@pytest.mark.parametrize("homog", [False, True])
+def test_mlp_gradient_matches_oracle(homog):
     P, ld = 1000, 1037
     p, X, T, isc, tsc = _mlp_case(P, ld, seed=5)
-    m = F.SubfilterStressMLP(params=p)
+    m = F.SubfilterStressMLP(params=p, homogeneous=homog)
     m.in_scale.copy_(_dev(isc))
     m.t_scale.copy_(_dev(tsc))
     g, loss = m.grad_of(_dev(X), _dev(T), ld, P)
     g = g.cpu().numpy().astype(np.float64)
-    le, ge = OC.mlp_loss_grad(p, X[:, :P], T[:, :P], isc, tsc, emulate_bf16=True)
-    l64, g64 = OC.mlp_loss_grad(p, X[:, :P], T[:, :P], isc, tsc)
+    le, ge = OC.mlp_loss_grad(p, X[:, :P], T[:, :P], isc, tsc, emulate_bf16=True, homogeneous=homog)
+    l64, g64 = OC.mlp_loss_grad(p, X[:, :P], T[:, :P], isc, tsc, homogeneous=homog)
     assert abs(float(loss.item()) - le) <= 1e-4 * le
     gd, ged, g64d = OC.mlp_unpack(g), OC.mlp_unpack(ge), OC.mlp_unpack(g64)
     for k in ("W1", "b1", "W2", "b2", "W3", "b3"):
@@ -349,10 +352,12 @@ def test_learned_closure_gain():
     F.evolve_forced_navier_stokes_device(u_dev, ks, 40, 5e-3, 2e-3, kf=2.0, power=0.1)
     d = F.closure_data(u_dev, ks, np.pi / 8)
     n = d.n
-    m = F.SubfilterStressMLP(seed=0)
-    hist = m.train(d, 0, n // 2, steps=600, batch=16384, lr=3e-3, log_every=100)
-    ev = m.evaluate(d, n // 2, n)
-    print(hist, ev)
-    assert hist[-1][1] < hist[0][1]
-    assert ev["rel_l2_mlp"] < 0.6 * ev["rel_l2_no_closure"]
-    assert ev["corr_mlp"] > 0.8
+    res = {}
+    for homog in (False, True):
+        m = F.SubfilterStressMLP(seed=0, homogeneous=homog)
+        hist = m.train(d, 0, n // 2, steps=800, batch=16384, lr=3e-3, log_every=100)
+        res[homog] = ev = m.evaluate(d, n // 2, n)
+        print(homog, hist, ev)
+        assert hist[-1][1] < hist[0][1]
+        assert ev["rel_l2_mlp"] < 0.6 * ev["rel_l2_no_closure"]
+        assert ev["corr_mlp"] > 0.75
