@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="s2s", choices=["s2s", "closure"],
+    ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch"],
                     help="s2s: the 512^3 shell-to-shell headline; closure: learned closure vs exact "
-                         "coarse-graining flux on a forced 256^3 field")
+                         "coarse-graining flux on a forced 256^3 field; batch: 64 uneven spectral-flux "
+                         "instances per graph launch")
+    ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--closure-n", type=int, default=256)
     ap.add_argument("--closure-nsteps", type=int, default=200)
     ap.add_argument("--train-steps", type=int, default=1500)
@@ -511,12 +513,191 @@ def run_closure(args):
     return 0
 
 
+def make_field_nd(ns, seed, device, spectrum, ncomp=None, project=True, dtype=None):
+    """Seeded Hermitian random-phase field û = fft(u)/Np on grid ns (any nd), shell spectrum
+    ``spectrum(|k|)`` (torch function), Leray-projected when ncomp == nd, mean removed. Returned as a
+    contiguous (ncomp, *reversed(ns)) CUDA tensor: the column-major (ns..., ncomp) layout."""
+    import torch
+    nd = len(ns)
+    ncomp = nd if ncomp is None else ncomp
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    shape = tuple(reversed(ns))
+    kk = []
+    for d in range(nd):
+        k1 = torch.fft.fftfreq(ns[d], d=1.0 / ns[d], device=device, dtype=torch.float64)
+        view = [1] * nd
+        view[nd - 1 - d] = ns[d]
+        kk.append(k1.view(view))
+    k2 = sum(k * k for k in kk)
+    km = torch.sqrt(k2)
+    amp = torch.where(km > 0, torch.sqrt(spectrum(km) / km.clamp_min(1e-30) ** (nd - 1)), torch.zeros_like(km))
+    Np = float(np.prod(ns))
+    u = torch.empty((ncomp,) + shape, dtype=torch.complex128, device=device)
+    for c in range(ncomp):
+        r = torch.randn(shape, generator=g, device=device, dtype=torch.float64)
+        u[c] = torch.fft.fftn(r) * (amp / Np)
+    if project and ncomp == nd:
+        div = sum(kk[d] * u[d] for d in range(nd)) / torch.where(k2 > 0, k2, torch.ones_like(k2))
+        for d in range(nd):
+            u[d] -= kk[d] * div
+    u[(slice(None),) + (0,) * nd] = 0
+    return u.to(dtype or torch.complex64).contiguous()
+
+
+def run_batch(args):
+    """64 uneven spectral-flux instances (half kinetic energy, half passive scalar; 2D 64^2..1024^2 and
+    3D 64^3..192^3, sizes 2^n and 3*2^n; isotropic / perpendicular / parallel shells) as ONE graph
+    launch in FP32 (FP64 shell sums), against the same set in FP64 for the per-instance error."""
+    import torch
+    import __graft_entry__
+    F = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(args.seed)
+    sizes2 = [64, 96, 128, 192, 256, 384, 512, 768, 1024]
+    sizes3 = [64, 96, 128, 192]
+    e_vel = lambda k: k ** 4 * torch.exp(-2 * (k / 4) ** 2)          # noqa: E731
+    e_sca = lambda k: k ** 2 * torch.exp(-(k / 6) ** 2)              # noqa: E731
+    geos = ["isotropic", "perpendicular", "parallel"]
+    specs32, specs64, desc = [], [], []
+    h2d = 0
+    for i in range(args.instances):
+        nd = 2 if i % 4 < 2 else 3
+        n = int(rng.choice(sizes2 if nd == 2 else sizes3))
+        ns = (n,) * nd
+        ks = F.wavenumber_grid(ns, (2 * np.pi,) * nd)
+        scalar = i % 2 == 1
+        gname = geos[int(rng.integers(0, 3))]
+        geo = {"isotropic": F.IsotropicShells(), "perpendicular": F.PerpendicularShells(),
+               "parallel": F.ParallelShells(dims=(nd,))}[gname]
+        u = make_field_nd(ns, args.seed * 1000 + 2 * i, dev, e_vel, dtype=torch.complex128)
+        th = make_field_nd(ns, args.seed * 1000 + 2 * i + 1, dev, e_sca, ncomp=1, project=False,
+                           dtype=torch.complex128) if scalar else None
+        base = {"ks": ks, "ns": ns, "geometry": geo, "binning": F.LinearBinning(1.0)}
+        specs64.append(dict(base, velocity_dev=u.view(-1), scalar_dev=th.view(-1) if scalar else None))
+        u32 = u.to(torch.complex64).view(-1)
+        th32 = th.to(torch.complex64).view(-1) if scalar else None
+        specs32.append(dict(base, velocity_dev=u32, scalar_dev=th32))
+        h2d += u32.numel() * 8 + (th32.numel() * 8 if scalar else 0)
+        desc.append(f"{'x'.join(map(str, ns))}:{'scalar' if scalar else 'ke'}:{gname}")
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    F.autotune_clear()
+    b32 = F.SpectralFluxBatch(specs32, precision=32, n_branches=4, autotune=True)
+    t0 = time.perf_counter()
+    b32.run()                                      # eager: allocation + autotuning
+    torch.cuda.synchronize()
+    tune_s = time.perf_counter() - t0
+    tune = F.autotune_summary()
+    b32.run()                                      # capture + launch
+    bus = None
+    try:
+        pr = torch.cuda.get_device_properties(dev)
+        bus = "%08X:%02X:%02X.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+    except Exception:
+        pass
+    clk = Clocks(bus)
+    clk.start()
+    l0 = F.launch_count()
+    ms_graph = timed(b32.run, args.steps)
+    launches = (F.launch_count() - l0) / (args.steps + max(3, args.warmup))
+    clocks = clk.stop()
+    ms_eager = timed(b32.run_eager, args.steps)
+    r32 = b32.results()
+    info = b32.info()
+    # same set, default kernels (autotuner off), graph
+    F.autotune_enable(False)
+    bnt = F.SpectralFluxBatch(specs32, precision=32, n_branches=4, autotune=False)
+    bnt.run()
+    bnt.run()
+    ms_graph_untuned = timed(bnt.run, args.steps)
+    bnt.close()
+    del bnt
+    # FP64 reference set (eager, plain FP64 path)
+    b64 = F.SpectralFluxBatch(specs64, precision=64, n_branches=1, autotune=False)
+    b64.run()
+    torch.cuda.synchronize()
+    ms64 = timed(b64.run_eager, 1)
+    r64 = b64.results()
+    b64.close()
+    errs = []
+    for a, b in zip(r32, r64):
+        errs.append(float(np.max(np.abs(a.transfer_spectrum.astype(np.float64) - b.transfer_spectrum)) /
+                         max(np.max(np.abs(b.transfer_spectrum)), 1e-300)))
+    # end to end: pinned host inputs -> device, one graph launch, T back to the host
+    hosts = [(s["velocity_dev"].cpu().pin_memory(), s["scalar_dev"].cpu().pin_memory() if s["scalar_dev"] is not None
+              else None) for s in specs32]
+    d2h = sum(int(it["T"].numel()) * 8 for it in b32.items)
+
+    def e2e_step():
+        for (hv, hs), it in zip(hosts, b32.items):
+            if hs is not None:
+                it["a"].copy_(hv, non_blocking=True)
+                it["f"].copy_(hs, non_blocking=True)
+            else:
+                it["f"].copy_(hv, non_blocking=True)
+        b32.run()
+        outs = [it["T"].to("cpu", non_blocking=True) for it in b32.items]
+        torch.cuda.synchronize()
+        return outs
+
+    for _ in range(2):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    n = len(specs32)
+    modes = sum(int(np.prod(s["ns"])) for s in specs32)
+    line = {"metric": f"uneven batch: {n} spectral-flux instances per graph launch (FP32, FP64 sums), instances/s",
+            "value": n / (ms_graph / 1e3), "unit": "instances/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{n} instances: 2D 64^2-1024^2 and 3D 64^3-192^3 (2^n, 3*2^n), half KE flux "
+                                   "(E ~ k^4 exp(-2(k/4)^2)) and half passive-scalar flux (k^2 exp(-(k/6)^2)); "
+                                   "isotropic / perpendicular / parallel shells, LinearBinning(1), 2/3 rule",
+                       "seed": args.seed, "instances": desc, "modes_total": modes,
+                       "l2": "inputs cycle through ~%.1f GB per launch (> 129 MB L2)" % (h2d / 1e9)},
+            "modes_per_s": modes / (ms_graph / 1e3),
+            "graph": {"kernels": info["graph_kernels"], "branches": info["branches"]},
+            "ms_sequential_eager_autotuned": ms_eager, "ms_graph_default_kernels": ms_graph_untuned,
+            "speedup_graph_vs_sequential": ms_eager / ms_graph,
+            "speedup_autotuned_vs_default_graph": ms_graph_untuned / ms_graph,
+            "autotune": {"entries": tune["entries"], "runtime_engine_chosen": tune["runtime_engine_chosen"],
+                         "tuning_s": tune_s, "sum_ms_default": tune["ms_default_sum"],
+                         "sum_ms_best": tune["ms_best_sum"]},
+            "fp64_plain_ms": ms64, "speedup_fp32_graph_vs_fp64": ms64 / ms_graph,
+            "rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
+            "e2e": {"value": n / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps},
+            "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    b32.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.config == "closure":
         return run_closure(args)
+    if args.config == "batch":
+        return run_batch(args)
     return run_ours(args)
 
 

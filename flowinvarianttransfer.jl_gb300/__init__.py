@@ -14,6 +14,8 @@ from .api import (compute_nonlinear_term, transfer_density, decompose_field, ass
                   calculate_helical_partial_fluxes, calculate_mode_to_mode_transfer,
                   calculate_scalar_mode_to_mode_transfer, calculate_energy_transfer)
 from .plan import Plan, get_plan, clear_plans  # noqa: F401
+from .batch import (SpectralFluxBatch, calculate_spectral_flux_batch, autotune_summary,  # noqa: F401
+                    autotune_enable, autotune_clear)
 from .closure import (calculate_coarse_graining_flux, evolve_forced_navier_stokes,  # noqa: F401
                       evolve_forced_navier_stokes_device, closure_data, ClosureData, SubfilterStressMLP,
                       gradient_model_flux, field_compare)

@@ -16,6 +16,8 @@ EXPORTS = [
     "fit_partial_fluxes", "fit_mode_to_mode", "fit_prof_enable", "fit_prof_read", "fit_prof_kind_name",
     "fit_coarse_graining_flux", "fit_forward_spectrum", "fit_ns_evolve", "fit_mlp_nparams", "fit_mlp_forward",
     "fit_mlp_train_grad", "fit_mlp_adam", "fit_gradient_model_flux", "fit_field_moments", "fit_field_compare",
+    "fit_batch_create", "fit_batch_destroy", "fit_batch_add_flux", "fit_batch_run", "fit_batch_run_eager", "fit_batch_info",
+    "fit_autotune_enable", "fit_autotune_clear", "fit_autotune_info", "fit_autotune_entry",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -63,6 +65,16 @@ def _declare(lib):
     lib.fit_gradient_model_flux.argtypes = [vp, i64, i64, C.c_double, vp, vp, vp]
     lib.fit_field_moments.argtypes = [vp, i64, i64, i32, vp, vp]
     lib.fit_field_compare.argtypes = [vp, vp, i64, vp, vp]
+    lib.fit_batch_create.argtypes = [C.POINTER(vp), i32]
+    lib.fit_batch_destroy.argtypes = [vp]
+    lib.fit_batch_add_flux.argtypes = [vp, vp, vp, vp, dp, i32, u32, i32, i32, vp, vp]
+    lib.fit_batch_run.argtypes = [vp, vp]
+    lib.fit_batch_run_eager.argtypes = [vp, vp]
+    lib.fit_batch_info.argtypes = [vp, C.POINTER(i64), i32]
+    lib.fit_autotune_enable.argtypes = [i32]
+    lib.fit_autotune_clear.argtypes = []
+    lib.fit_autotune_info.argtypes = [C.POINTER(i64), C.POINTER(i64), dp, dp]
+    lib.fit_autotune_entry.argtypes = [i64, C.POINTER(i64), dp]
     lib.fit_mlp_adam.argtypes = [vp, vp, vp, vp, i32, f32, f32, f32, f32, vp]
     for name in EXPORTS:
         if name not in ("fit_last_error", "fit_launch_count", "fit_prof_kind_name"):

@@ -228,7 +228,7 @@ static int check_invariant(const fit_plan* p, int inv, int ncomp) {
 }
 
 template <typename T>
-static int carrier_and_bin_setup(fit_plan* p, const void* carrier, int inv) {
+int fit::carrier_and_bin_setup(fit_plan* p, const void* carrier, int inv) {
   typedef typename Vec2<T>::t V;
   FIT_TRY(ensure(p, &p->ceff, sizeof(V) * 3 * p->g.Mhalf));
   FIT_TRY(ensure(p, &p->seff, sizeof(uint16_t) * p->g.Mhalf));
@@ -238,13 +238,18 @@ static int carrier_and_bin_setup(fit_plan* p, const void* carrier, int inv) {
 }
 
 template <typename T>
-static int bin_into(fit_plan* p, const void* nh, long bstride, int nb, const void* ceff, double* out) {
+int fit::bin_into(fit_plan* p, const void* nh, long bstride, int nb, const void* ceff, double* out) {
   typedef typename Vec2<T>::t V;
   const long cap = 2L * 152 * nb * p->nsh;
   FIT_TRY(ensure(p, &p->partial, sizeof(double) * cap));
   return bin_density<T>(p->g, (const V*)nh, bstride, nb, (const V*)ceff, p->M, (const uint16_t*)p->seff.p, p->nsh,
                         (double*)p->partial.p, cap, out, p->stream);
 }
+
+template int fit::carrier_and_bin_setup<float>(fit_plan*, const void*, int);
+template int fit::carrier_and_bin_setup<double>(fit_plan*, const void*, int);
+template int fit::bin_into<float>(fit_plan*, const void*, long, int, const void*, double*);
+template int fit::bin_into<double>(fit_plan*, const void*, long, int, const void*, double*);
 
 // ---- C ABI ------------------------------------------------------------------------------------
 

@@ -41,6 +41,12 @@ template <typename T>
 int forward_nd(const T* phys, typename Vec2<T>::t* half, const GridDesc& g, const Axis* ax, long nf, T scale,
                cudaStream_t st);
 
+// Pass autotuner (fit_passes.cu): on/off, reset, summary and per-entry readout.
+void autotune_enable(bool on);
+void autotune_clear();
+void autotune_summary(long* n, long* changed, double* ms_default, double* ms_best);
+bool autotune_entry(long i, long* fields, float* ms_best, float* ms_default);
+
 // ---- pointwise / reduction kernels (fit_ops.cu) ----------------------------------------------
 
 // Wavenumber tables of the data grid (FP64, FFTW order) as device pointers.

@@ -2,8 +2,12 @@
 #include <math.h>
 #include <stdlib.h>
 
+#include <array>
+#include <atomic>
+#include <map>
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include "fit_fft.cuh"
 #include "fit_ops.cuh"
@@ -142,6 +146,261 @@ static int prep_kernel(K kern, size_t smem) {
   return FIT_OK;
 }
 
+// ---- autotuner -------------------------------------------------------------------------------
+// For each pass shape (kind, N, columns/lines, batch, element size) the first call outside a graph
+// capture times every candidate kernel on scratch buffers and keeps the fastest: the compile-time
+// engine (fixed tile) and the runtime engine over tile widths C (powers of two), elements per
+// thread (8, 16) and radix orders (8s first, 4s first, 8s last). Later calls, captured or not,
+// launch the recorded choice. Off unless enabled (fit_autotune_enable).
+
+enum PassKind { PASS_FWD = 0, PASS_INV = 1, PASS_C2R = 2, PASS_R2C = 3 };
+
+struct Cand {
+  int engine;   // 0 compile-time kernel, 1 runtime kernel
+  int C, ept, sched;
+};
+
+struct TuneEntry {
+  Cand best;
+  float ms_best, ms_default;
+  int ncand;
+};
+
+static std::atomic<int> g_tune_on(0);
+static std::mutex g_tune_mu;
+static std::map<std::array<long, 5>, TuneEntry> g_tune;
+
+// Radix order: 0 = 8s, then 4|2, 3s, 5s; 1 = 4s, then 2, 3s, 5s; 2 = order 0 reversed.
+static bool make_sched(int N, int sched, Radices* rd) {
+  int n = N, p2 = 0, n3 = 0, n5 = 0, ns = 0;
+  while (n % 2 == 0) { n /= 2; ++p2; }
+  while (n % 3 == 0) { n /= 3; ++n3; }
+  while (n % 5 == 0) { n /= 5; ++n5; }
+  if (n != 1) return false;
+  int r[32];
+  if (sched == 1) {
+    for (int i = 0; i < p2 / 2; ++i) r[ns++] = 4;
+    if (p2 % 2) r[ns++] = 2;
+  } else {
+    for (int i = 0; i < p2 / 3; ++i) r[ns++] = 8;
+    if (p2 % 3 == 2) r[ns++] = 4;
+    if (p2 % 3 == 1) r[ns++] = 2;
+  }
+  for (int i = 0; i < n3; ++i) r[ns++] = 3;
+  for (int i = 0; i < n5; ++i) r[ns++] = 5;
+  if (ns > 16) return false;
+  rd->n = ns;
+  for (int i = 0; i < ns; ++i) rd->r[i] = sched == 2 ? r[ns - 1 - i] : r[i];
+  return true;
+}
+
+static bool is_capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return true;   // unknown: behave as if capturing (no tuning)
+  }
+  return cs != cudaStreamCaptureStatusNone;
+}
+
+// Launch one candidate. Returns FIT_OK, 1 (candidate not available) or an error code.
+template <typename T>
+static int launch_cand(int kind, const void* in, void* out, const Axis& ax, long P, long Q, T scale, const Cand& c,
+                       cudaStream_t st) {
+  typedef typename Vec2<T>::t V;
+  const V* tw = axis_tw<T>(ax);
+  const int N = ax.N;
+  if (c.engine == 0) {
+    if (kind == PASS_FWD || kind == PASS_INV)
+      return ct_strided<T>((const V*)in, (V*)out, N, P, Q, kind == PASS_INV, scale, tw, st);
+    if (kind == PASS_C2R) return ct_c2r<T>((const V*)in, (T*)out, N, P, scale, tw, st);
+    return ct_r2c<T>((const T*)in, (V*)out, N, P, scale, tw, st);
+  }
+  Radices rd;
+  if (!make_sched(N, c.sched, &rd)) return 1;
+  const long E = (long)c.C * N;
+  long nthr = (E + c.ept - 1) / c.ept;
+  nthr = ((nthr + 31) / 32) * 32;
+  if (nthr < 32) nthr = 32;
+  const size_t smem = (size_t)(E + N) * sizeof(V);
+  if (nthr > 1024 || smem > 200 * 1024) return 1;
+  if (kind == PASS_FWD || kind == PASS_INV) {
+    const long tpq = (P + c.C - 1) / c.C;
+    const long grid = tpq * Q;
+    if (grid > 2147483647L) return 1;
+#define FIT_TS(INV, EPT)                                                                                      \
+  do {                                                                                                        \
+    FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, smem));                                                  \
+    k_pass_strided<V, INV, EPT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const V*)in, (V*)out, N, P, tpq, \
+                                                                               c.C, rd, tw, scale);           \
+  } while (0)
+    if (kind == PASS_INV) {
+      if (c.ept == 8) FIT_TS(true, 8); else FIT_TS(true, 16);
+    } else {
+      if (c.ept == 8) FIT_TS(false, 8); else FIT_TS(false, 16);
+    }
+#undef FIT_TS
+    return FIT_OK;
+  }
+  const long grid = (P + 2L * c.C - 1) / (2L * c.C);
+  if (kind == PASS_C2R) {
+    if (c.ept == 8) {
+      FIT_TRY(prep_kernel(k_c2r_x<V, 8>, smem));
+      k_c2r_x<V, 8><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const V*)in, (T*)out, N, P, c.C, rd, tw, scale);
+    } else {
+      FIT_TRY(prep_kernel(k_c2r_x<V, 16>, smem));
+      k_c2r_x<V, 16><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const V*)in, (T*)out, N, P, c.C, rd, tw, scale);
+    }
+  } else {
+    if (c.ept == 8) {
+      FIT_TRY(prep_kernel(k_r2c_x<V, 8>, smem));
+      k_r2c_x<V, 8><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const T*)in, (V*)out, N, P, c.C, rd, tw, scale);
+    } else {
+      FIT_TRY(prep_kernel(k_r2c_x<V, 16>, smem));
+      k_r2c_x<V, 16><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const T*)in, (V*)out, N, P, c.C, rd, tw, scale);
+    }
+  }
+  return FIT_OK;
+}
+
+// Bytes of the input and output buffers of a pass (P columns or lines, Q batches).
+template <typename T>
+static void pass_bytes(int kind, int N, long P, long Q, size_t* bin, size_t* bout) {
+  typedef typename Vec2<T>::t V;
+  if (kind == PASS_FWD || kind == PASS_INV) {
+    *bin = *bout = sizeof(V) * (size_t)P * N * Q;
+  } else if (kind == PASS_C2R) {
+    *bin = sizeof(V) * (size_t)P * (N / 2 + 1);
+    *bout = sizeof(T) * (size_t)P * N;
+  } else {
+    *bin = sizeof(T) * (size_t)P * N;
+    *bout = sizeof(V) * (size_t)P * (N / 2 + 1);
+  }
+}
+
+// The choice for this pass shape: true with *c set when the tuner is on and a choice exists (made
+// now if needed and possible); false means "use the default path".
+template <typename T>
+static bool tune_pick(int kind, const Axis& ax, long P, long Q, T scale, cudaStream_t st, Cand* c) {
+  typedef typename Vec2<T>::t V;
+  if (!g_tune_on.load()) return false;
+  const std::array<long, 5> key = {kind, ax.N, P, Q, (long)sizeof(V)};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      *c = it->second.best;
+      return true;
+    }
+  }
+  if (is_capturing(st)) return false;
+  // Scratch: the batch dimension Q is cut so a tuning buffer stays under 256 MB (every block
+  // handles one (tile, q) pair, so per-q cost is what is compared).
+  long Qt = Q;
+  size_t bin, bout;
+  pass_bytes<T>(kind, ax.N, P, 1, &bin, &bout);
+  const size_t cap = 256u << 20;
+  if (kind == PASS_FWD || kind == PASS_INV) {
+    while (Qt > 1 && bin * Qt > cap) Qt = (Qt + 1) / 2;
+  }
+  pass_bytes<T>(kind, ax.N, P, Qt, &bin, &bout);
+  void *sin = nullptr, *sout = nullptr;
+  if (cudaMalloc(&sin, bin) != cudaSuccess || cudaMalloc(&sout, bout) != cudaSuccess) {
+    cudaGetLastError();
+    if (sin) cudaFree(sin);
+    return false;
+  }
+  cudaMemsetAsync(sin, 0, bin, st);
+  std::vector<Cand> cands;
+  cands.push_back(Cand{0, 0, 0, 0});
+  const int vb = (int)sizeof(V);
+  for (int C = 1; C <= 256; C *= 2) {
+    if ((long)C * ax.N * vb > 192 * 1024) break;
+    for (int ept : {8, 16})
+      for (int sched = 0; sched < 3; ++sched) cands.push_back(Cand{1, C, ept, sched});
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  TuneEntry best;
+  best.ms_best = 1e30f;
+  best.ms_default = -1.f;
+  best.ncand = 0;
+  best.best = Cand{0, 0, 0, 0};
+  bool have = false;
+  for (const Cand& cd : cands) {
+    if (cd.engine == 1 && cd.C > 1) {
+      const long cols = (kind == PASS_FWD || kind == PASS_INV) ? P : (P + 1) / 2;
+      long ap2 = 1;
+      while (ap2 < cols) ap2 *= 2;
+      if (cd.C > ap2) continue;   // wider than the columns (line pairs) that exist
+    }
+    int rc = launch_cand<T>(kind, sin, sout, ax, P, Qt, scale, cd, st);
+    if (rc == 1) continue;
+    if (rc != FIT_OK || cudaGetLastError() != cudaSuccess) continue;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 3; ++r) launch_cand<T>(kind, sin, sout, ax, P, Qt, scale, cd, st);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= 3.f;
+    best.ncand++;
+    if (cd.engine == 0 && best.ms_default < 0.f) best.ms_default = ms;
+    if (ms < best.ms_best) {
+      best.ms_best = ms;
+      best.best = cd;
+      have = true;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sin);
+  cudaFree(sout);
+  if (!have) return false;
+  if (best.ms_default < 0.f) best.ms_default = best.ms_best;   // no compile-time kernel for this length
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = best;
+  *c = best.best;
+  return true;
+}
+
+void autotune_enable(bool on) { g_tune_on.store(on ? 1 : 0); }
+
+void autotune_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+}
+
+// entries, entries whose choice is not the compile-time kernel, sum of default ms, sum of best ms
+void autotune_summary(long* n, long* changed, double* ms_default, double* ms_best) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  *n = (long)g_tune.size();
+  *changed = 0;
+  *ms_default = *ms_best = 0.0;
+  for (auto& kv : g_tune) {
+    if (kv.second.best.engine != 0) ++*changed;
+    *ms_default += kv.second.ms_default;
+    *ms_best += kv.second.ms_best;
+  }
+}
+
+// Entry i: kind, N, P, Q, element bytes, engine, C, ept, sched; times in ms.
+bool autotune_entry(long i, long* fields, float* ms_best, float* ms_default) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (i < 0 || i >= (long)g_tune.size()) return false;
+  auto it = g_tune.begin();
+  std::advance(it, i);
+  for (int k = 0; k < 5; ++k) fields[k] = it->first[k];
+  fields[5] = it->second.best.engine;
+  fields[6] = it->second.best.C;
+  fields[7] = it->second.best.ept;
+  fields[8] = it->second.best.sched;
+  *ms_best = it->second.ms_best;
+  *ms_default = it->second.ms_default;
+  return true;
+}
+
 template <typename T>
 int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const Axis& ax, long P, long Q,
                  bool inverse, T scale, cudaStream_t st) {
@@ -160,6 +419,18 @@ int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const 
   }
   const V* tw = axis_tw<T>(ax);
   fit_prof_begin(PK_FFT_STRIDED, 2.0 * (double)P * ax.N * Q * sizeof(V), st);
+  {
+    Cand c;
+    if (tune_pick<T>(inverse ? PASS_INV : PASS_FWD, ax, P, Q, scale, st, &c)) {
+      const int rc = launch_cand<T>(inverse ? PASS_INV : PASS_FWD, in, out, ax, P, Q, scale, c, st);
+      if (rc == FIT_OK) {
+        fit_prof_end(st);
+        FIT_LAUNCH_CHECK();
+        return FIT_OK;
+      }
+      if (rc != 1) return rc;
+    }
+  }
   {
     const int rc = ct_strided<T>(in, out, ax.N, P, Q, inverse, scale, tw, st);
     if (rc != 1) {
@@ -195,6 +466,18 @@ int pass_c2r_x(const typename Vec2<T>::t* in, T* out, const Axis& ax, long L, T 
   const V* tw = axis_tw<T>(ax);
   fit_prof_begin(PK_FFT_C2R_X, (double)L * ((ax.N / 2 + 1) * sizeof(V) + ax.N * sizeof(T)), st);
   {
+    Cand c;
+    if (tune_pick<T>(PASS_C2R, ax, L, 1, scale, st, &c)) {
+      const int rc = launch_cand<T>(PASS_C2R, in, out, ax, L, 1, scale, c, st);
+      if (rc == FIT_OK) {
+        fit_prof_end(st);
+        FIT_LAUNCH_CHECK();
+        return FIT_OK;
+      }
+      if (rc != 1) return rc;
+    }
+  }
+  {
     const int rc = ct_c2r<T>(in, out, ax.N, L, scale, tw, st);
     if (rc != 1) {
       fit_prof_end(st);
@@ -223,6 +506,18 @@ int pass_r2c_x(const T* in, typename Vec2<T>::t* out, const Axis& ax, long L, T 
   const long grid = (L + 2L * t.C - 1) / (2L * t.C);
   const V* tw = axis_tw<T>(ax);
   fit_prof_begin(PK_FFT_R2C_X, (double)L * ((ax.N / 2 + 1) * sizeof(V) + ax.N * sizeof(T)), st);
+  {
+    Cand c;
+    if (tune_pick<T>(PASS_R2C, ax, L, 1, scale, st, &c)) {
+      const int rc = launch_cand<T>(PASS_R2C, in, out, ax, L, 1, scale, c, st);
+      if (rc == FIT_OK) {
+        fit_prof_end(st);
+        FIT_LAUNCH_CHECK();
+        return FIT_OK;
+      }
+      if (rc != 1) return rc;
+    }
+  }
   {
     const int rc = ct_r2c<T>(in, out, ax.N, L, scale, tw, st);
     if (rc != 1) {

@@ -49,6 +49,12 @@ int ensure(fit_plan* p, fit_dbuf* b, size_t bytes);
 int ensure_shells(fit_plan* p, const double* edges, int n_edges, unsigned dims, int coord_f32);
 template <typename T>
 int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u);
+// Effective carrier + shell map of the plan's transform grid, and shell sums of a half-spectrum
+// product against it (fit_api.cu).
+template <typename T>
+int carrier_and_bin_setup(fit_plan* p, const void* carrier, int inv);
+template <typename T>
+int bin_into(fit_plan* p, const void* nh, long bstride, int nb, const void* ceff, double* out);
 int s2s_batched(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, double* Tdev);
 int s2s_check(fit_plan* p);
 void s2s_free(fit_plan* p);

@@ -154,6 +154,36 @@ int fit_forward_spectrum(fit_plan* plan, const void* u_phys, void* u_hat, int pt
 int fit_ns_evolve(fit_plan* plan, void* u_hat, int nsteps, double dt, double nu, double kf, double power,
                   int ptr_kind);
 
+/* ---- uneven batches and the transform autotuner --------------------------------------------------
+ * A batch runs many spectral-flux instances, each calculate_spectral_flux / calculate_scalar_flux
+ * (src/SpectralFlux.jl:49-94,148-180,203-269) on its own plan (grid, dimension, invariant, shell
+ * geometry and edges may all differ), as one CUDA graph launch. The reference computes such a set
+ * one call at a time; batching has no counterpart there. Pointers are device pointers fixed when
+ * the instance is added; T_dev / Pi_dev receive n_edges-1 doubles (Pi_dev may be NULL). The first
+ * fit_batch_run executes eagerly (allocation, autotuning), the second captures the graph over
+ * n_branches concurrent branch streams and launches it, later runs only launch it. Runs are
+ * asynchronous on `stream`. */
+typedef struct fit_batch fit_batch;
+int fit_batch_create(fit_batch** out, int n_branches);
+int fit_batch_destroy(fit_batch* batch);
+int fit_batch_add_flux(fit_batch* batch, fit_plan* plan, const void* u_dev, const void* adv_dev, const double* edges,
+                       int n_edges, uint32_t dims_mask, int coord_f32, int invariant, double* T_dev, double* Pi_dev);
+int fit_batch_run(fit_batch* batch, void* stream);
+/* Every instance launched eagerly, one after the other on `stream` (no graph): the sequential form. */
+int fit_batch_run_eager(fit_batch* batch, void* stream);
+/* out[0..3] = instances, state (0 new, 1 eager run done, 2 graph ready), kernels in the graph, branches */
+int fit_batch_info(const fit_batch* batch, int64_t* out, int n);
+
+/* Transform-pass autotuner (global, off by default): when on, the first launch of every pass shape
+ * outside a graph capture times the candidate kernels (compile-time engine; runtime engine over
+ * tile widths, elements per thread and radix orders) and keeps the fastest for later launches. */
+int fit_autotune_enable(int on);
+int fit_autotune_clear(void);
+int fit_autotune_info(int64_t* n_entries, int64_t* n_runtime_engine, double* ms_default, double* ms_best);
+/* fields[0..8] = kind (0 fwd, 1 inv strided, 2 c2r, 3 r2c), N, columns or lines, batch, element
+ * bytes, engine (0 compile-time, 1 runtime), C, elements per thread, radix order; ms = best, default. */
+int fit_autotune_entry(int64_t i, int64_t* fields, double* ms);
+
 /* ---- learned subfilter-stress closure (no counterpart in the reference) -------------------------
  * A pointwise MLP 9 -> 64 -> 64 -> 6 (ReLU) maps the filtered velocity-gradient tensor A_ij = d_j ū_i
  * (9 features) to the six subfilter-stress components (tau_00 tau_11 tau_22 tau_01 tau_02 tau_12).
