@@ -11,7 +11,7 @@ from .shells import (wavenumber_grid, shell_edges, shell_centers, n_shells, defa
 from .api import (compute_nonlinear_term, transfer_density, decompose_field, assign_shells_device,  # noqa: F401
                   calculate_spectral_flux, calculate_scalar_flux, calculate_shell_to_shell_transfer,
                   calculate_scalar_shell_to_shell_transfer, calculate_partial_fluxes,
-                  calculate_helical_partial_fluxes, calculate_mode_to_mode_transfer,
+                  calculate_helical_partial_fluxes, calculate_partial_fluxes_multi, calculate_mode_to_mode_transfer,
                   calculate_scalar_mode_to_mode_transfer, calculate_energy_transfer)
 from .plan import Plan, get_plan, clear_plans  # noqa: F401
 from .batch import (SpectralFluxBatch, calculate_spectral_flux_batch, autotune_summary,  # noqa: F401

@@ -162,19 +162,39 @@ def calculate_scalar_shell_to_shell_transfer(velocity_hat, scalar_hat, ks, **kw)
 
 
 # ---- partial fluxes --------------------------------------------------------------------------------
+def _decomposition_code(decomposition):
+    if isinstance(decomposition, HelicalDecomposition):
+        return 1, HelicalDecomposition.names
+    if isinstance(decomposition, HelmholtzDecomposition):
+        return 2, HelmholtzDecomposition.names
+    raise ValueError("calculate_partial_fluxes needs a decomposition that splits u into ≥2 named components "
+                     f"(e.g. HelicalDecomposition or HelmholtzDecomposition); got {type(decomposition).__name__}.")
+
+
+def _partial_result(Tc, names, centers, ft):
+    chans = {}
+    for sk in range(2):
+        for sp in range(2):
+            for sq in range(2):
+                T = Tc[sk * 4 + sp * 2 + sq].astype(ft)
+                chans[(names[sk], names[sp], names[sq])] = SpectralFluxResult(centers.astype(ft), T, np.cumsum(T))
+    tot_T = sum(c.transfer_spectrum for c in chans.values())
+    tot_P = sum(c.flux for c in chans.values())
+    return PartialFluxResult(chans, SpectralFluxResult(centers.astype(ft), tot_T, tot_P), centers.astype(ft))
+
+
 def calculate_partial_fluxes(velocity_hat, ks, decomposition=HelicalDecomposition(), binning=None,
                              dealiasing=OrszagTwoThirds(), spectral=GB300Spectral(), geometry=IsotropicShells(),
-                             invariant=KineticEnergy()):
+                             invariant=KineticEnergy(), execution=None):
     """``calculate_partial_fluxes`` (``src/SpectralFlux.jl:240-285``): 8 channels (sk, sp, sq) plus the
-    total. ``invariant=Helicity()`` swaps the density of ``:277`` (helical helicity channels)."""
+    total. ``invariant=Helicity()`` swaps the density of ``:277`` (helical helicity channels).
+    ``execution=GB300Execution("batched")`` uses the one-pass, graph-replayed form."""
+    if isinstance(execution, GB300Execution) and execution.mode == "batched":
+        return calculate_partial_fluxes_multi(velocity_hat, ks, invariants=(invariant,), decomposition=decomposition,
+                                              binning=binning, dealiasing=dealiasing, spectral=spectral,
+                                              geometry=geometry)[type(invariant).__name__]
     v = np.asarray(velocity_hat)
-    if isinstance(decomposition, HelicalDecomposition):
-        code, names = 1, HelicalDecomposition.names
-    elif isinstance(decomposition, HelmholtzDecomposition):
-        code, names = 2, HelmholtzDecomposition.names
-    else:
-        raise ValueError("calculate_partial_fluxes needs a decomposition that splits u into ≥2 named components "
-                         f"(e.g. HelicalDecomposition or HelmholtzDecomposition); got {type(decomposition).__name__}.")
+    code, names = _decomposition_code(decomposition)
     binning, edges, centers, dm, f32 = _shells(ks, binning, geometry)
     ft = _ft(v)
     p = _plan(v, ks, dealiasing, spectral, None)
@@ -188,6 +208,21 @@ def calculate_partial_fluxes(velocity_hat, ks, decomposition=HelicalDecompositio
     tot_T = sum(c.transfer_spectrum for c in chans.values())
     tot_P = sum(c.flux for c in chans.values())
     return PartialFluxResult(chans, SpectralFluxResult(centers.astype(ft), tot_T, tot_P), centers.astype(ft))
+
+
+def calculate_partial_fluxes_multi(velocity_hat, ks, invariants=(KineticEnergy(), Helicity()),
+                                   decomposition=HelicalDecomposition(), binning=None, dealiasing=OrszagTwoThirds(),
+                                   spectral=GB300Spectral(), geometry=IsotropicShells()):
+    """The 8 channels of every invariant in ``invariants`` from one pass over the components (the four
+    nonlinear terms are shared), replayed as one CUDA graph from the second call on. Returns
+    ``{invariant type name: PartialFluxResult}``, each as ``calculate_partial_fluxes`` would."""
+    v = np.asarray(velocity_hat)
+    code, names = _decomposition_code(decomposition)
+    binning, edges, centers, dm, f32 = _shells(ks, binning, geometry)
+    ft = _ft(v)
+    p = _plan(v, ks, dealiasing, spectral, None)
+    Tc = p.partial_fluxes_batched(v, code, [i.code for i in invariants], edges, dm, f32)
+    return {type(inv).__name__: _partial_result(Tc[j], names, centers, ft) for j, inv in enumerate(invariants)}
 
 
 def calculate_helical_partial_fluxes(velocity_hat, ks, **kw):

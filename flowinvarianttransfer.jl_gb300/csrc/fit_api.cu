@@ -377,6 +377,7 @@ int fit_plan_destroy(fit_plan* p) {
   if (!p) return FIT_OK;
   if (p->stream) cudaStreamSynchronize(p->stream);
   s2s_free(p);
+  partial_free(p);
   fit_dbuf* bufs[] = {&p->in_u, &p->in_a, &p->in_c, &p->out_c, &p->out_c2, &p->hs, &p->ph, &p->nph, &p->nh,
                       &p->ceff, &p->seff, &p->partial, &p->outd, &p->shell_full, &p->edges_dev};
   for (fit_dbuf* b : bufs) release(b);
@@ -396,6 +397,7 @@ int fit_plan_set_stream(fit_plan* p, void* stream) {
   p->own_stream = false;
   p->stream = (cudaStream_t)stream;
   s2s_free(p);   // captured graphs belong to the old stream
+  partial_free(p);
   return FIT_OK;
 }
 

@@ -54,15 +54,28 @@ FIT_D void map_pair(const GridDesc& g, int g0, int g1, int g2, KIdx* kA, KIdx* k
 // Orszag 2/3 keep predicate on the N grid (src/NonlinearTerm.jl:134-141): every axis index
 // magnitude below N_d div 3.
 FIT_D bool keep23(const GridDesc& g, const int* k) {
-  for (int d = 0; d < g.nd; ++d) {
-    const int N = g.N[d];
-    const int a = (k[d] <= N / 2) ? k[d] : N - k[d];
-    if (a >= N / 3) return false;
+  bool keep = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {   // unrolled: k stays in registers
+    if (d < g.nd) {
+      const int N = g.N[d];
+      const int a = (k[d] <= N / 2) ? k[d] : N - k[d];
+      keep = keep && a < N / 3;
+    }
   }
-  return true;
+  return keep;
 }
 
 FIT_D void decode_half(const GridDesc& g, long i, int* g0, int* g1, int* g2) {
+  if (g.Mhalf <= 0x7fffffffL) {   // 32-bit index arithmetic (every grid up to 1024^3 fits)
+    const unsigned u = (unsigned)i, m0 = (unsigned)g.Mh0, m1 = (unsigned)g.M[1];
+    const unsigned r = u / m0;
+    const unsigned q = r / m1;
+    *g0 = (int)(u - r * m0);
+    *g1 = (int)(r - q * m1);
+    *g2 = (int)q;
+    return;
+  }
   *g0 = (int)(i % g.Mh0);
   const long r = i / g.Mh0;
   *g1 = (int)(r % g.M[1]);
@@ -89,37 +102,79 @@ FIT_D double2 dmul_i(double2 a, double k) { return make_double2(-a.y * k, a.x * 
 //   KE / passive scalar: C = u;   helicity: C = i k x u;
 //   enstrophy 2D: w = i(kx uy - ky ux), C = (w * i ky, -w * i kx);   enstrophy 3D: C = ik x (ik x u).
 
-FIT_D void carrier_at(const GridDesc& g, const KTab& kt, const void* car, int f64, long cs, int nc, int inv,
-                      long lin, const int* k, double2* C) {
-  double2 u[3];
-  for (int c = 0; c < nc && c < 3; ++c) u[c] = ld_c(car, f64, lin + cs * c);
+// CT: arithmetic type (float for single-precision data, double otherwise).
+template <typename CT>
+FIT_D typename Vec2<CT>::t ld_ct(const void* p, int f64, long i) {
+  typename Vec2<CT>::t r;
+  if (f64) {
+    const double2 v = reinterpret_cast<const double2*>(p)[i];
+    r.x = (CT)v.x;
+    r.y = (CT)v.y;
+  } else {
+    const float2 v = reinterpret_cast<const float2*>(p)[i];
+    r.x = (CT)v.x;
+    r.y = (CT)v.y;
+  }
+  return r;
+}
+
+template <typename CT>
+FIT_D void carrier_at_t(const GridDesc& g, const KTab& kt, const void* car, int f64, long cs, int nc, int inv,
+                        long lin, const int* k, typename Vec2<CT>::t* C) {
+  typedef typename Vec2<CT>::t C2;
+  C2 u[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = c < nc ? ld_ct<CT>(car, f64, lin + cs * c) : mkc<C2>(0, 0);
   if (inv == INV_KE || inv == INV_SCALAR) {
-    for (int c = 0; c < nc; ++c) C[c] = u[c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if (c < nc) C[c] = u[c];
     return;
   }
-  const double kx = kt.k[0][k[0]];
-  const double ky = g.nd >= 2 ? kt.k[1][k[1]] : 0.0;
-  const double kz = g.nd >= 3 ? kt.k[2][k[2]] : 0.0;
+  const CT kx = (CT)kt.k[0][k[0]];
+  const CT ky = g.nd >= 2 ? (CT)kt.k[1][k[1]] : (CT)0;
+  const CT kz = g.nd >= 3 ? (CT)kt.k[2][k[2]] : (CT)0;
   if (inv == INV_ENSTROPHY && g.nd == 2) {
     // w = i (kx uy - ky ux)
-    const double2 w = make_double2(-(kx * u[1].y - ky * u[0].y), kx * u[1].x - ky * u[0].x);
-    C[0] = dmul_i(w, ky);
-    C[1] = dmul_i(w, -kx);
+    const C2 w = mkc<C2>(-(kx * u[1].y - ky * u[0].y), kx * u[1].x - ky * u[0].x);
+    C[0] = mkc<C2>(-w.y * ky, w.x * ky);
+    C[1] = mkc<C2>(w.y * kx, -w.x * kx);
     return;
   }
   // curl: i (k x u)
-  double2 w[3];
-  w[0] = make_double2(-(ky * u[2].y - kz * u[1].y), ky * u[2].x - kz * u[1].x);
-  w[1] = make_double2(-(kz * u[0].y - kx * u[2].y), kz * u[0].x - kx * u[2].x);
-  w[2] = make_double2(-(kx * u[1].y - ky * u[0].y), kx * u[1].x - ky * u[0].x);
+  C2 w[3];
+  w[0] = mkc<C2>(-(ky * u[2].y - kz * u[1].y), ky * u[2].x - kz * u[1].x);
+  w[1] = mkc<C2>(-(kz * u[0].y - kx * u[2].y), kz * u[0].x - kx * u[2].x);
+  w[2] = mkc<C2>(-(kx * u[1].y - ky * u[0].y), kx * u[1].x - ky * u[0].x);
   if (inv == INV_HELICITY) {
     C[0] = w[0]; C[1] = w[1]; C[2] = w[2];
     return;
   }
-  C[0] = make_double2(-(ky * w[2].y - kz * w[1].y), ky * w[2].x - kz * w[1].x);
-  C[1] = make_double2(-(kz * w[0].y - kx * w[2].y), kz * w[0].x - kx * w[2].x);
-  C[2] = make_double2(-(kx * w[1].y - ky * w[0].y), kx * w[1].x - ky * w[0].x);
+  C[0] = mkc<C2>(-(ky * w[2].y - kz * w[1].y), ky * w[2].x - kz * w[1].x);
+  C[1] = mkc<C2>(-(kz * w[0].y - kx * w[2].y), kz * w[0].x - kx * w[2].x);
+  C[2] = mkc<C2>(-(kx * w[1].y - ky * w[0].y), kx * w[1].x - ky * w[0].x);
 }
 
+FIT_D void carrier_at(const GridDesc& g, const KTab& kt, const void* car, int f64, long cs, int nc, int inv,
+                      long lin, const int* k, double2* C) {
+  carrier_at_t<double>(g, kt, car, f64, cs, nc, inv, lin, k, C);
+}
+
+// N-grid linear index -> per-axis indices (32-bit arithmetic when the grid allows it).
+FIT_D void decode_full(const GridDesc& g, long i, int* k) {
+  if (g.Ntot <= 0x7fffffffL) {
+    const unsigned u = (unsigned)i, n0 = (unsigned)g.N[0], n1 = (unsigned)g.N[1];
+    const unsigned r = u / n0;
+    const unsigned q = r / n1;
+    k[0] = (int)(u - r * n0);
+    k[1] = (int)(r - q * n1);
+    k[2] = (int)q;
+    return;
+  }
+  k[0] = (int)(i % g.N[0]);
+  const long r = i / g.N[0];
+  k[1] = (int)(r % g.N[1]);
+  k[2] = (int)(r / g.N[1]);
+}
 
 }  // namespace fit

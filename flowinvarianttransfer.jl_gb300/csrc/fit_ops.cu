@@ -24,40 +24,85 @@ static inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b);
 
 // ---- Hermitian gather ------------------------------------------------------------------------
 
-template <typename V>
-__global__ void k_gather(GridDesc g, KTab kt, GatherArgs a, V* out) {
+// One thread per half-spectrum mode, looping over the fields: the index maps, 2/3 predicate, shell
+// lookups, wavenumbers and filter response are computed once per mode and reused by every field.
+// CT is the arithmetic type: FP32 when both the source and the output are single precision (the
+// result is rounded to FP32 anyway), FP64 otherwise.
+template <typename V, typename CT>
+__global__ void __launch_bounds__(256) k_gather(GridDesc g, KTab kt, GatherArgs a, V* out) {
+  typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= g.Mhalf) return;
-  const GatherField f = a.f[blockIdx.y];
   int g0, g1, g2;
   decode_half(g, i, &g0, &g1, &g2);
   KIdx kk[2];
   map_pair(g, g0, g1, g2, &kk[0], &kk[1]);
-  double2 acc = make_double2(0.0, 0.0);
+  bool ok[2];
+  CT kd[2][3], G[2] = {(CT)1, (CT)1};
+  int sh[2] = {0, 0};
+  bool any_band = false, any_filt = false;
+#pragma unroll
+  for (int f = 0; f < 16; ++f) {
+    if (f < a.nfields) {
+      any_band |= a.f[f].band > 0;
+      any_filt |= a.f[f].filt != 0;
+    }
+  }
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
-    const KIdx& k = kk[s];
-    if (k.lin < 0) continue;
-    if (a.two_thirds && !keep23(g, k.k)) continue;
-    if (f.band > 0 && a.shell_full[k.lin] != f.band) continue;
-    double2 v = ld_c(a.src[f.src], a.in_f64, k.lin + a.src_comp_stride[f.src] * f.comp);
-    if (f.deriv >= 0) v = dmul_i(v, kt.k[f.deriv][k.k[f.deriv]]);
-    if (f.filt) {
-      double k2 = 0.0;
-      for (int d = 0; d < g.nd; ++d) {
-        const double kd = kt.k[d][k.k[d]];
-        k2 += kd * kd;
-      }
-      const double G = filter_response(a.filter_kind, sqrt(k2), a.ell);
-      v.x *= G;
-      v.y *= G;
+    ok[s] = kk[s].lin >= 0 && (!a.two_thirds || keep23(g, kk[s].k));
+    double k2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double kv = (d < g.nd && ok[s]) ? kt.k[d][kk[s].k[d]] : 0.0;
+      kd[s][d] = (CT)kv;
+      k2 += kv * kv;
     }
-    if (s == 1) v.y = -v.y;
-    acc.x += v.x;
-    acc.y += v.y;
+    if (ok[s] && any_band) sh[s] = a.shell_full[kk[s].lin];
+    if (ok[s] && any_filt) G[s] = (CT)filter_response(a.filter_kind, sqrt(k2), a.ell);
   }
-  const double sc = 0.5 * a.scale;
-  out[(long)blockIdx.y * g.Mhalf + i] = to_v<V>(make_double2(acc.x * sc, acc.y * sc));
+  const CT sc = (CT)(0.5 * a.scale);
+#pragma unroll
+  for (int f = 0; f < 16; ++f) {   // unrolled: compile-time indices into the parameter block
+    if (f >= a.nfields) break;
+    const GatherField fd = a.f[f];
+    CT ax = 0, ay = 0;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      if (!ok[s] || (fd.band > 0 && sh[s] != fd.band)) continue;
+      const void* src = fd.src ? a.src[1] : a.src[0];
+      const long idx = kk[s].lin + (fd.src ? a.src_comp_stride[1] : a.src_comp_stride[0]) * fd.comp;
+      CT vx, vy;
+      if (a.in_f64) {
+        const double2 v = reinterpret_cast<const double2*>(src)[idx];
+        vx = (CT)v.x;
+        vy = (CT)v.y;
+      } else {
+        const float2 v = reinterpret_cast<const float2*>(src)[idx];
+        vx = (CT)v.x;
+        vy = (CT)v.y;
+      }
+      if (fd.deriv >= 0) {   // i k v
+        const CT k = fd.deriv == 0 ? kd[s][0] : (fd.deriv == 1 ? kd[s][1] : kd[s][2]);
+        const CT tx = -vy * k;
+        vy = vx * k;
+        vx = tx;
+      }
+      if (fd.filt) {
+        vx *= G[s];
+        vy *= G[s];
+      }
+      ax += vx;
+      ay += s == 1 ? -vy : vy;
+    }
+    C2 r;
+    r.x = ax * sc;
+    r.y = ay * sc;
+    V o;
+    o.x = (typename Scal<V>::t)r.x;
+    o.y = (typename Scal<V>::t)r.y;
+    out[(long)f * g.Mhalf + i] = o;
+  }
 }
 
 template <typename T>
@@ -66,9 +111,11 @@ int gather_half(const GridDesc& g, const KTab& kt, const GatherArgs& a, typename
     fit_set_error("gather: bad field count %d", a.nfields);
     return FIT_ERR_ARG;
   }
-  dim3 grid(nblk(g.Mhalf, 256), a.nfields);
   fit_prof_begin(PK_GATHER, (double)a.nfields * g.Mhalf * (sizeof(typename Vec2<T>::t) + 2.0 * (a.in_f64 ? 16 : 8)), st);
-  k_gather<typename Vec2<T>::t><<<grid, 256, 0, st>>>(g, kt, a, out);
+  if (sizeof(T) == 4 && !a.in_f64)
+    k_gather<typename Vec2<T>::t, float><<<nblk(g.Mhalf, 256), 256, 0, st>>>(g, kt, a, out);
+  else
+    k_gather<typename Vec2<T>::t, double><<<nblk(g.Mhalf, 256), 256, 0, st>>>(g, kt, a, out);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
@@ -82,10 +129,13 @@ __global__ void k_product(const T* __restrict__ u, const T* __restrict__ grad, T
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   T uu[3];
-  for (int j = 0; j < nd; ++j) uu[j] = u[(long)j * n + i];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) uu[j] = j < nd ? u[(long)j * n + i] : (T)0;
   for (int c = 0; c < M; ++c) {
     T s = (T)0;
-    for (int j = 0; j < nd; ++j) s += uu[j] * grad[(long)(c * nd + j) * n + i];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (j < nd) s += uu[j] * grad[(long)(c * nd + j) * n + i];
     out[(long)c * n + i] = s;
   }
 }
@@ -104,9 +154,11 @@ int product(const T* u, const T* grad, T* out, int nd, int M, long n, cudaStream
 // space, so N(-g) = conj(N(g))). Term A covers N-grid modes with non-negative x frequency, term
 // B those with negative x frequency (never counted twice). seff = shell of those modes (equal for
 // A and B: shells are symmetric under k -> -k), 0 when masked or absent.
-template <typename V>
-__global__ void k_ceff(GridDesc g, KTab kt, const void* car, int f64, long cs, int ncar, int inv, int two_thirds,
-                       const uint16_t* __restrict__ shell, V* ceff, int nce, uint16_t* seff) {
+template <typename V, typename CT>
+__global__ void __launch_bounds__(256) k_ceff(GridDesc g, KTab kt, const void* car, int f64, long cs, int ncar, int inv,
+                                              int two_thirds, const uint16_t* __restrict__ shell, V* ceff, int nce,
+                                              uint16_t* seff) {
+  typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= g.Mhalf) return;
   int g0, g1, g2;
@@ -122,14 +174,21 @@ __global__ void k_ceff(GridDesc g, KTab kt, const void* car, int f64, long cs, i
     const int* kk = A ? kA.k : kB.k;
     if ((A || B) && !keep23(g, kk)) s = 0;
   }
-  double2 CA[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-  double2 CB[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+  C2 CA[3], CB[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) CA[c] = CB[c] = mkc<C2>(0, 0);
   if (s != 0) {
-    if (A) carrier_at(g, kt, car, f64, cs, ncar, inv, kA.lin, kA.k, CA);
-    if (B) carrier_at(g, kt, car, f64, cs, ncar, inv, kB.lin, kB.k, CB);
+    if (A) carrier_at_t<CT>(g, kt, car, f64, cs, ncar, inv, kA.lin, kA.k, CA);
+    if (B) carrier_at_t<CT>(g, kt, car, f64, cs, ncar, inv, kB.lin, kB.k, CB);
   }
-  for (int c = 0; c < nce; ++c)
-    ceff[(long)c * g.Mhalf + i] = to_v<V>(make_double2(CA[c].x + CB[c].x, CA[c].y - CB[c].y));
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (c < nce) {
+      V o;
+      o.x = (typename Scal<V>::t)(CA[c].x + CB[c].x);
+      o.y = (typename Scal<V>::t)(CA[c].y - CB[c].y);
+      ceff[(long)c * g.Mhalf + i] = o;
+    }
   seff[i] = s;
 }
 
@@ -142,22 +201,32 @@ int effective_carrier(const GridDesc& g, const KTab& kt, const void* carrier, in
     return FIT_ERR_ARG;
   }
   fit_prof_begin(PK_CARRIER, (double)g.Mhalf * nceff * (sizeof(typename Vec2<T>::t) + 2.0 * (in_f64 ? 16 : 8)), st);
-  k_ceff<typename Vec2<T>::t><<<nblk(g.Mhalf, 256), 256, 0, st>>>(g, kt, carrier, in_f64, comp_stride, ncomp_carrier,
-                                                                 invariant, two_thirds, shell_full, ceff, nceff, seff);
+  if (sizeof(T) == 4 && !in_f64)
+    k_ceff<typename Vec2<T>::t, float><<<nblk(g.Mhalf, 256), 256, 0, st>>>(
+        g, kt, carrier, in_f64, comp_stride, ncomp_carrier, invariant, two_thirds, shell_full, ceff, nceff, seff);
+  else
+    k_ceff<typename Vec2<T>::t, double><<<nblk(g.Mhalf, 256), 256, 0, st>>>(
+        g, kt, carrier, in_f64, comp_stride, ncomp_carrier, invariant, two_thirds, shell_full, ceff, nceff, seff);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
 
 // ---- shell binning ----------------------------------------------------------------------------
-// Block-local FP64 bins in shared memory (lanes with the same shell are combined with warp
-// shuffles first), per-block partials, then a fixed-order reduction over blocks.
+// Block-local FP64 bins in shared memory, per-block partials, then a fixed-order reduction over
+// blocks. Runs of equal shells in consecutive lanes (modes along a row are ordered by |k|) are first
+// summed by a log-step segmented warp reduction, so only each run's first lane touches the bins.
+// The per-mode products and the in-warp run sums use CT: FP64 for FP64 data; FP32 for FP32 data
+// (inputs carry FP32 rounding already; at most 32 terms per run), with every run sum accumulated
+// in FP64 from there on. nset carrier sets (ceff_set_stride elements apart) are binned against the
+// same N̂ in one pass.
 
-template <typename V>
-__global__ void k_bin(const V* __restrict__ nh, long bstride, int nb, const V* __restrict__ ceff, int nc,
-                      const uint16_t* __restrict__ seff, long Mhalf, int nsh, double* __restrict__ partial) {
+template <typename V, typename CT>
+__global__ void __launch_bounds__(256) k_bin(const V* __restrict__ nh, long bstride, int nb, const V* __restrict__ ceff,
+                                             long cstride, int nset, int nc, const uint16_t* __restrict__ seff,
+                                             long Mhalf, int nsh, double* __restrict__ partial) {
   extern __shared__ double bins[];
-  const int nbins = nb * nsh;
+  const int nbins = nset * nb * nsh;
   for (int t = threadIdx.x; t < nbins; t += blockDim.x) bins[t] = 0.0;
   __syncthreads();
   const long step = (long)gridDim.x * blockDim.x;
@@ -165,44 +234,63 @@ __global__ void k_bin(const V* __restrict__ nh, long bstride, int nb, const V* _
   const unsigned lane = threadIdx.x & 31;
   for (long it = 0; it < iters; ++it) {
     const long i = it * step + blockIdx.x * (long)blockDim.x + threadIdx.x;
-    int s = 0;
-    V cf[3];
-    if (i < Mhalf) {
-      s = seff[i];
-      if (s) for (int c = 0; c < nc; ++c) cf[c] = ceff[(long)c * Mhalf + i];
-    }
-    const unsigned grp = __match_any_sync(0xffffffffu, s);
-    const int leader = __ffs(grp) - 1;
+    const int s = (i < Mhalf) ? (int)seff[i] : 0;
+    const int sr = __shfl_down_sync(0xffffffffu, s, 1);
+    const int sl = __shfl_up_sync(0xffffffffu, s, 1);
+    const unsigned same_right = __ballot_sync(0xffffffffu, lane < 31 && sr == s);
+    const int run_end = __ffs(~same_right & (0xffffffffu << lane)) - 1;
+    const bool head = lane == 0 || sl != s;
     for (int b = 0; b < nb; ++b) {
-      double v = 0.0;
-      if (s) {
-        for (int c = 0; c < nc; ++c) {
-          const V x = nh[b * bstride + (long)c * Mhalf + i];
-          v += (double)cf[c].x * (double)x.x + (double)cf[c].y * (double)x.y;
-        }
+      V x[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        x[c].x = x[c].y = 0;
+        if (s && c < nc) x[c] = nh[b * bstride + (long)c * Mhalf + i];
       }
-      double sum = 0.0;
-      for (unsigned m = grp; m; m &= m - 1) sum += __shfl_sync(grp, v, __ffs(m) - 1);
-      if (s && (int)lane == leader) atomicAdd(&bins[b * nsh + (s - 1)], sum);
+      for (int m = 0; m < nset; ++m) {
+        CT v = 0;
+        if (s) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            if (c < nc) {
+              const V cf = ceff[m * cstride + (long)c * Mhalf + i];
+              v += (CT)cf.x * (CT)x[c].x + (CT)cf.y * (CT)x[c].y;
+            }
+          }
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const CT t = __shfl_down_sync(0xffffffffu, v, off);
+          if ((int)lane + off <= run_end) v += t;
+        }
+        if (s && head) atomicAdd(&bins[(m * nb + b) * nsh + (s - 1)], (double)v);
+      }
     }
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nbins; t += blockDim.x) partial[(long)blockIdx.x * nbins + t] = bins[t];
 }
 
-__global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks, int nbins, double* out) {
+// out[set][b*nsh + n] = sum over blocks of partial[block][(set*nb + b)*nsh + n]
+__global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks, int nbins, int per_set,
+                                  BinOut out) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nbins) return;
   double s = 0.0;
   for (int b = 0; b < nblocks; ++b) s += partial[(long)b * nbins + j];
-  out[j] = s;
+  out.p[j / per_set][j % per_set] = s;
 }
 
 template <typename T>
-int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,
-                const typename Vec2<T>::t* ceff, int nc, const uint16_t* seff, int nsh, double* partial,
-                long partial_cap, double* out, cudaStream_t st) {
-  const int nbins = nb * nsh;
+int bin_density_multi(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,
+                      const typename Vec2<T>::t* ceff, long ceff_set_stride, int nset, int nc, const uint16_t* seff,
+                      int nsh, double* partial, long partial_cap, const BinOut& out, cudaStream_t st) {
+  typedef typename Vec2<T>::t V;
+  if (nset < 1 || nset > 8) {
+    fit_set_error("binning: 1..8 carrier sets per pass (got %d)", nset);
+    return FIT_ERR_ARG;
+  }
+  const int nbins = nset * nb * nsh;
   const size_t smem = sizeof(double) * nbins;
   if (smem > 96 * 1024) {
     fit_set_error("too many shell bins (%d) for one binning launch", nbins);
@@ -216,22 +304,36 @@ int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_
     fit_set_error("binning scratch too small");
     return FIT_ERR_SIZE;
   }
+  const bool f32 = sizeof(T) == 4;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_bin<typename Vec2<T>::t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = f32 ? cudaFuncSetAttribute(k_bin<V, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(k_bin<V, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {
       fit_set_error("cudaFuncSetAttribute failed: %s", cudaGetErrorString(e));
       return FIT_ERR_CUDA;
     }
   }
-  fit_prof_begin(PK_BIN, (double)g.Mhalf * ((nb + 1) * nc * sizeof(typename Vec2<T>::t) + 2.0), st);
-  k_bin<typename Vec2<T>::t><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, nc, seff, g.Mhalf, nsh,
-                                                        partial);
+  fit_prof_begin(PK_BIN, (double)g.Mhalf * ((nb + nset) * nc * sizeof(V) + 2.0), st);
+  if (f32)
+    k_bin<V, float><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, ceff_set_stride, nset, nc, seff, g.Mhalf,
+                                               nsh, partial);
+  else
+    k_bin<V, double><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, ceff_set_stride, nset, nc, seff,
+                                                g.Mhalf, nsh, partial);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
-  k_reduce_partials<<<nblk(nbins, 128), 128, 0, st>>>(partial, nblocks, nbins, out);
+  k_reduce_partials<<<nblk(nbins, 128), 128, 0, st>>>(partial, nblocks, nbins, nb * nsh, out);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
+}
+
+template <typename T>
+int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,
+                const typename Vec2<T>::t* ceff, int nc, const uint16_t* seff, int nsh, double* partial,
+                long partial_cap, double* out, cudaStream_t st) {
+  BinOut o;
+  o.p[0] = out;
+  return bin_density_multi<T>(g, nh, nh_batch_stride, nb, ceff, 0, 1, nc, seff, nsh, partial, partial_cap, o, st);
 }
 
 // ---- scatter to the full N-grid user layout ---------------------------------------------------
@@ -388,44 +490,56 @@ FIT_D void st_c(void* p, int f64, long i, double2 v) {
 
 // Craya-Herring basis per mode, as src/Decomposition.jl:63-98 (reference vector z unless
 // |khat_z| >= 0.9, then x; the mean mode carries nothing).
-__global__ void k_helical(GridDesc g, KTab kt, const void* u, int f64, void* up, void* um) {
+// Arithmetic in CT: FP32 for single-precision fields, FP64 otherwise. The split is invariant under
+// the choice of the transverse pair (e1, e2): a rotation of the pair multiplies h+- by a phase and
+// the coefficients by its conjugate.
+template <typename CT>
+__global__ void __launch_bounds__(256) k_helical(GridDesc g, KTab kt, const void* u, int f64, void* up, void* um) {
+  typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= g.Ntot) return;
   int k[3];
-  k[0] = (int)(i % g.N[0]);
-  const long r = i / g.N[0];
-  k[1] = (int)(r % g.N[1]);
-  k[2] = (int)(r / g.N[1]);
-  const double kx = kt.k[0][k[0]], ky = kt.k[1][k[1]], kz = kt.k[2][k[2]];
-  const double kk = sqrt(kx * kx + ky * ky + kz * kz);
+  decode_full(g, i, k);
+  const CT kx = (CT)kt.k[0][k[0]], ky = (CT)kt.k[1][k[1]], kz = (CT)kt.k[2][k[2]];
+  const CT kk = sqrt(kx * kx + ky * ky + kz * kz);
   const long n = g.Ntot;
-  if (kk == 0.0) {
+  C2 P[3], Mv[3];
+  if (kk == (CT)0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) P[c] = Mv[c] = mkc<C2>(0, 0);
+  } else {
+    const CT hx = kx / kk, hy = ky / kk, hz = kz / kk;
+    CT rx = 0, ry = 0, rz = 1;
+    if (!(fabs(hz) < (CT)0.9)) { rx = 1; rz = 0; }
+    CT e1x = hy * rz - hz * ry, e1y = hz * rx - hx * rz, e1z = hx * ry - hy * rx;
+    const CT n1 = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+    e1x /= n1; e1y /= n1; e1z /= n1;
+    const CT e2x = hy * e1z - hz * e1y, e2y = hz * e1x - hx * e1z, e2z = hx * e1y - hy * e1x;
+    const C2 u1 = ld_ct<CT>(u, f64, i), u2 = ld_ct<CT>(u, f64, i + n), u3 = ld_ct<CT>(u, f64, i + 2 * n);
+    const C2 ue1 = mkc<C2>(u1.x * e1x + u2.x * e1y + u3.x * e1z, u1.y * e1x + u2.y * e1y + u3.y * e1z);
+    const C2 ue2 = mkc<C2>(u1.x * e2x + u2.x * e2y + u3.x * e2z, u1.y * e2x + u2.y * e2y + u3.y * e2z);
+    const CT is2 = (CT)0.70710678118654752440;
+    // u+ coefficient (ue1 - i ue2)/sqrt2, u- coefficient (ue1 + i ue2)/sqrt2
+    const C2 upc = mkc<C2>((ue1.x + ue2.y) * is2, (ue1.y - ue2.x) * is2);
+    const C2 umc = mkc<C2>((ue1.x - ue2.y) * is2, (ue1.y + ue2.x) * is2);
+    const CT e1[3] = {e1x, e1y, e1z}, e2[3] = {e2x, e2y, e2z};
+#pragma unroll
     for (int c = 0; c < 3; ++c) {
-      st_c(up, f64, i + n * c, make_double2(0, 0));
-      st_c(um, f64, i + n * c, make_double2(0, 0));
+      const C2 hp = mkc<C2>(e1[c] * is2, e2[c] * is2);    // (e1 + i e2)/sqrt2
+      const C2 hm = mkc<C2>(e1[c] * is2, -e2[c] * is2);   // (e1 - i e2)/sqrt2
+      P[c] = mkc<C2>(upc.x * hp.x - upc.y * hp.y, upc.x * hp.y + upc.y * hp.x);
+      Mv[c] = mkc<C2>(umc.x * hm.x - umc.y * hm.y, umc.x * hm.y + umc.y * hm.x);
     }
-    return;
   }
-  const double hx = kx / kk, hy = ky / kk, hz = kz / kk;
-  double rx = 0, ry = 0, rz = 1;
-  if (!(fabs(hz) < 0.9)) { rx = 1; rz = 0; }
-  double e1x = hy * rz - hz * ry, e1y = hz * rx - hx * rz, e1z = hx * ry - hy * rx;
-  const double n1 = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
-  e1x /= n1; e1y /= n1; e1z /= n1;
-  const double e2x = hy * e1z - hz * e1y, e2y = hz * e1x - hx * e1z, e2z = hx * e1y - hy * e1x;
-  const double2 u1 = ld_c(u, f64, i), u2 = ld_c(u, f64, i + n), u3 = ld_c(u, f64, i + 2 * n);
-  const double2 ue1 = make_double2(u1.x * e1x + u2.x * e1y + u3.x * e1z, u1.y * e1x + u2.y * e1y + u3.y * e1z);
-  const double2 ue2 = make_double2(u1.x * e2x + u2.x * e2y + u3.x * e2z, u1.y * e2x + u2.y * e2y + u3.y * e2z);
-  const double is2 = 1.0 / sqrt(2.0);
-  // u+ coefficient (ue1 - i ue2)/sqrt2, u- coefficient (ue1 + i ue2)/sqrt2
-  const double2 upc = make_double2((ue1.x + ue2.y) * is2, (ue1.y - ue2.x) * is2);
-  const double2 umc = make_double2((ue1.x - ue2.y) * is2, (ue1.y + ue2.x) * is2);
-  const double e1[3] = {e1x, e1y, e1z}, e2[3] = {e2x, e2y, e2z};
+#pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const double2 hp = make_double2(e1[c] * is2, e2[c] * is2);    // (e1 + i e2)/sqrt2
-    const double2 hm = make_double2(e1[c] * is2, -e2[c] * is2);   // (e1 - i e2)/sqrt2
-    st_c(up, f64, i + n * c, make_double2(upc.x * hp.x - upc.y * hp.y, upc.x * hp.y + upc.y * hp.x));
-    st_c(um, f64, i + n * c, make_double2(umc.x * hm.x - umc.y * hm.y, umc.x * hm.y + umc.y * hm.x));
+    if (f64) {
+      reinterpret_cast<double2*>(up)[i + n * c] = make_double2((double)P[c].x, (double)P[c].y);
+      reinterpret_cast<double2*>(um)[i + n * c] = make_double2((double)Mv[c].x, (double)Mv[c].y);
+    } else {
+      reinterpret_cast<float2*>(up)[i + n * c] = make_float2((float)P[c].x, (float)P[c].y);
+      reinterpret_cast<float2*>(um)[i + n * c] = make_float2((float)Mv[c].x, (float)Mv[c].y);
+    }
   }
 }
 
@@ -434,7 +548,8 @@ int helical_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, 
     fit_set_error("HelicalDecomposition is defined in 3D only (got nd=%d).", g.nd);
     return FIT_ERR_ARG;
   }
-  k_helical<<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um);
+  if (in_f64) k_helical<double><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um);
+  else k_helical<float><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -491,6 +606,10 @@ template int effective_carrier<float>(const GridDesc&, const KTab&, const void*,
                                       const uint16_t*, float2*, int, uint16_t*, cudaStream_t);
 template int effective_carrier<double>(const GridDesc&, const KTab&, const void*, int, long, int, int, int,
                                        const uint16_t*, double2*, int, uint16_t*, cudaStream_t);
+template int bin_density_multi<float>(const GridDesc&, const float2*, long, int, const float2*, long, int, int,
+                                      const uint16_t*, int, double*, long, const BinOut&, cudaStream_t);
+template int bin_density_multi<double>(const GridDesc&, const double2*, long, int, const double2*, long, int, int,
+                                       const uint16_t*, int, double*, long, const BinOut&, cudaStream_t);
 template int bin_density<float>(const GridDesc&, const float2*, long, int, const float2*, int, const uint16_t*, int,
                                 double*, long, double*, cudaStream_t);
 template int bin_density<double>(const GridDesc&, const double2*, long, int, const double2*, int, const uint16_t*,

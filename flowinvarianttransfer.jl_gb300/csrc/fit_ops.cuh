@@ -100,6 +100,18 @@ int effective_carrier(const GridDesc& g, const KTab& kt, const void* carrier, in
                       int ncomp_carrier, int invariant, int two_thirds, const uint16_t* shell_full,
                       typename Vec2<T>::t* ceff, int nceff, uint16_t* seff, cudaStream_t st);
 
+// Output rows of a multi-carrier binning pass: set m writes out.p[m][b*nsh + n].
+struct BinOut {
+  double* p[8];
+};
+
+// Shell sums of nset carrier sets against the same N̂ in one pass:
+// out.p[m][b*nsh + n] = sum_{g: seff(g)=n+1} sum_c Re(conj(ceff_m,c(g)) * nh_b,c(g)).
+template <typename T>
+int bin_density_multi(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,
+                      const typename Vec2<T>::t* ceff, long ceff_set_stride, int nset, int nc, const uint16_t* seff,
+                      int nsh, double* partial, long partial_cap, const BinOut& out, cudaStream_t st);
+
 // Shell sums: out[b*nsh + n] = sum_{g: seff(g)=n+1} sum_c Re(conj(ceff_c(g)) * nh_b,c(g)).
 template <typename T>
 int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,

@@ -42,6 +42,8 @@ struct fit_plan {
   int nsh = 0;
   // batched shell-to-shell state (fit_s2s.cu)
   void* s2s = nullptr;
+  // batched partial-flux state (fit_partial.cu)
+  void* partial_state = nullptr;
 };
 
 namespace fit {
@@ -58,5 +60,6 @@ int bin_into(fit_plan* p, const void* nh, long bstride, int nb, const void* ceff
 int s2s_batched(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, double* Tdev);
 int s2s_check(fit_plan* p);
 void s2s_free(fit_plan* p);
+void partial_free(fit_plan* p);
 int triad_m2m(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, int fp64, double* S, double* net);
 }  // namespace fit

@@ -148,6 +148,28 @@ class Plan:
                                               int(coord_f32), self._vp(out), PTR_HOST))
         return out.reshape(8, n)
 
+    def partial_fluxes_batched(self, u_hat, decomposition, invs, edges, dmask, coord_f32):
+        u = self._field(u_hat, self.M)
+        e = np.ascontiguousarray(edges, dtype=np.float64)
+        n = len(e) - 1
+        iv = (C.c_int * len(invs))(*invs)
+        out = np.zeros(len(invs) * 8 * n)
+        with self.lock:
+            check(self.lib.fit_partial_fluxes_batched(self.h, self._vp(u), decomposition, iv, len(invs), _dptr(e),
+                                                      len(e), dmask, int(coord_f32), self._vp(out), PTR_HOST))
+        return out.reshape(len(invs), 8, n)
+
+    def partial_fluxes_device(self, u_ptr, decomposition, inv, edges, dmask, coord_f32, T_ptr):
+        e = np.ascontiguousarray(edges, dtype=np.float64)
+        check(self.lib.fit_partial_fluxes(self.h, C.c_void_p(u_ptr), decomposition, inv, _dptr(e), len(e), dmask,
+                                          int(coord_f32), C.c_void_p(T_ptr), PTR_DEVICE))
+
+    def partial_fluxes_batched_device(self, u_ptr, decomposition, invs, edges, dmask, coord_f32, T_ptr):
+        e = np.ascontiguousarray(edges, dtype=np.float64)
+        iv = (C.c_int * len(invs))(*invs)
+        check(self.lib.fit_partial_fluxes_batched(self.h, C.c_void_p(u_ptr), decomposition, iv, len(invs), _dptr(e),
+                                                  len(e), dmask, int(coord_f32), C.c_void_p(T_ptr), PTR_DEVICE))
+
     def mode_to_mode(self, u_hat, inv, fp64=True, adv_hat=None):
         u = self._field(u_hat, self.M)
         a = None if adv_hat is None else self._field(adv_hat, self.D)

@@ -125,6 +125,16 @@ int fit_helmholtz_decompose(fit_plan* plan, const void* u_hat, void* u_rot, void
 int fit_partial_fluxes(fit_plan* plan, const void* u_hat, int decomposition, int invariant, const double* edges,
                        int n_edges, uint32_t dims_mask, int coord_f32, double* T_channels, int ptr_kind);
 
+/* The 8 partial-flux channels of n_invariants invariants (KE, Helicity, Enstrophy codes) from one
+ * pass: calculate_partial_fluxes (src/SpectralFlux.jl:240-285) for each invariant, sharing the four
+ * nonlinear terms (u_sp . grad) u_sq between invariants and the component transforms between
+ * terms. T_channels[(j*8 + sk*4 + sp*2 + sq)*nsh + n] for invariant j. The first call for a set of
+ * pointers runs eagerly, the second captures a CUDA graph (on a plan stream other than the legacy
+ * default stream), later calls replay it. */
+int fit_partial_fluxes_batched(fit_plan* plan, const void* u_hat, int decomposition, const int* invariants,
+                               int n_invariants, const double* edges, int n_edges, uint32_t dims_mask, int coord_f32,
+                               double* T_channels, int ptr_kind);
+
 /* Resolved S(k|p) (column-major [k..., p...]) and net(k) = sum_p S(k|p). Replaces
  * calculate_mode_to_mode_transfer (src/ScaleToScale/ScaleToScaleTransfer.jl:49-91).
  * fp64_products = 1 evaluates every triad in FP64, 0 in FP32 with FP64 sums. */
