@@ -49,11 +49,12 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial"],
+    ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial", "padded", "m2m"],
                     help="s2s: the 512^3 shell-to-shell headline; closure: learned closure vs exact "
                          "coarse-graining flux on a forced 256^3 field; batch: 64 uneven spectral-flux "
                          "instances per graph launch; partial: 512^3 helical partial fluxes of kinetic energy "
-                         "and helicity (16 channels) in one graph launch")
+                         "and helicity (16 channels) in one graph launch; padded: 256^3 32-shell shell-to-shell "
+                         "with the exact 3/2 rule; m2m: 32^3 resolved mode-to-mode S(k|p)")
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--closure-n", type=int, default=256)
     ap.add_argument("--closure-nsteps", type=int, default=200)
@@ -809,6 +810,139 @@ def run_partial(args):
     return 0
 
 
+def _timed_ms(fn, stream, reps, warm=1):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_padded(args):
+    """256^3 D=3 32-shell shell-to-shell with the exact 3/2 rule (384^3 transforms), field
+    E ~ k^4 exp(-2 (k/8)^2): FP32-batched vs plain FP64; antisymmetry and per-shell error."""
+    import torch
+    import __graft_entry__
+    F = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    N = 256
+    ns = (N, N, N)
+    ks = F.wavenumber_grid(ns, (2 * np.pi,) * 3)
+    edges = np.asarray(F.shell_edges(F.LinearBinning(7.0), F.kmax(ks)), dtype=np.float64)
+    nsh = len(edges) - 1
+    u = make_field(N, args.seed, dev, spectrum="k4exp8")
+    stream = torch.cuda.Stream(device=dev)
+    plan = F.Plan(ns, 3, 3, "three_halves", 32, False, ks)
+    plan.set_stream(stream.cuda_stream)
+    T = torch.zeros((nsh, nsh), dtype=torch.float64, device=dev)
+    net = torch.zeros(nsh, dtype=torch.float64, device=dev)
+    asym = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def step():
+        plan.shell_to_shell_device(u.data_ptr(), 0, edges, 7, 0, 0, F._lib.S2S_BATCHED, T.data_ptr(),
+                                   net.data_ptr(), asym.data_ptr())
+
+    l0 = F.launch_count()
+    ms = _timed_ms(step, stream, args.steps, warm=max(3, args.warmup))
+    launches = (F.launch_count() - l0) / (args.steps + max(3, args.warmup))
+    T32 = T.cpu().numpy().copy()
+    net32 = net.cpu().numpy().copy()
+    del plan
+    F.clear_plans()
+    torch.cuda.empty_cache()
+    u64 = u.to(torch.complex128)
+    p64 = F.Plan(ns, 3, 3, "three_halves", 64, True, ks)
+    p64.set_stream(stream.cuda_stream)
+    T64 = torch.zeros((nsh, nsh), dtype=torch.float64, device=dev)
+    ms64 = _timed_ms(lambda: p64.shell_to_shell_device(u64.data_ptr(), 0, edges, 7, 0, 0, F._lib.S2S_PLAIN,
+                                                        T64.data_ptr(), 0, 0), stream, 1, warm=1)
+    T64n = T64.cpu().numpy()
+    scale = np.max(np.abs(T64n))
+    line = {"metric": "256^3 3/2-padded 32-shell shell-to-shell T(n,m)/s: FP32-batched vs FP64 plain",
+            "value": 1000.0 / ms, "unit": "T(n,m)/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"256^3 D=3 {nsh}-shell shell-to-shell, LinearBinning(7), PaddedThreeHalves "
+                                   "(384^3 transforms), E ~ k^4 exp(-2(k/8)^2), FP32-batched with FP64 sums",
+                       "seed": args.seed},
+            "fp64_plain_ms": ms64, "speedup_vs_fp64_plain": ms64 / ms,
+            "rel_err_vs_fp64_maxnorm": float(np.max(np.abs(T32 - T64n)) / scale),
+            "per_shell_rel_err_max_over_shells_with_transfer": float(np.max(
+                (np.abs(T32 - T64n).max(axis=0) / np.maximum(np.abs(T64n).max(axis=0), 1e-300))[
+                    np.abs(T64n).max(axis=0) > 1e-3 * scale])),
+            "antisymmetry_fp32_rel": float(np.max(np.abs(T32 + T32.T)) / scale),
+            "antisymmetry_fp64_rel": float(np.max(np.abs(T64n + T64n.T)) / scale),
+            "conservation_fp32": float(abs(net32.sum()) / np.abs(T32).sum()),
+            "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_m2m(args):
+    """32^3 D=3 resolved mode-to-mode S(k|p) (32768^2 = 1.07e9 pairs, FP64 sums, 8.6 GB output),
+    E ~ k^4 exp(-2 (k/8)^2), 2/3 rule; shell sums of S against T(n,m) of the shell-to-shell path."""
+    import torch
+    import __graft_entry__
+    F = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    N = 32
+    ns = (N, N, N)
+    nm = N ** 3
+    ks = F.wavenumber_grid(ns, (2 * np.pi,) * 3)
+    u = make_field(N, args.seed, dev, spectrum="k4exp8").to(torch.complex128).contiguous()
+    stream = torch.cuda.Stream(device=dev)
+    plan = F.Plan(ns, 3, 3, "two_thirds", 64, True, ks)
+    plan.set_stream(stream.cuda_stream)
+    S = torch.empty((nm, nm), dtype=torch.float64, device=dev)
+    net = torch.empty(nm, dtype=torch.float64, device=dev)
+    res = {}
+    for fp64 in (True, False):
+        ms = _timed_ms(lambda: plan.mode_to_mode_device(u.data_ptr(), 0, fp64, S.data_ptr(), net.data_ptr()),
+                       stream, max(1, args.steps), warm=2)
+        res["fp64_products" if fp64 else "fp32_products"] = {
+            "ms": ms, "pairs_per_s": nm * nm / (ms / 1e3), "GBps_S_write": 8.0 * nm * nm / (ms / 1e3) / 1e9}
+    # shell sums of S (FP64 products) against T(n,m)
+    plan.mode_to_mode_device(u.data_ptr(), 0, True, S.data_ptr(), net.data_ptr())
+    edges = np.asarray(F.shell_edges(F.LinearBinning(1.0), F.kmax(ks)), dtype=np.float64)
+    nsh = len(edges) - 1
+    idx = torch.from_numpy(plan.assign_shells(edges, 7, False).ravel(order="F")).to(dev)
+    valid = idx > 0
+    oh = torch.zeros((nsh, nm), dtype=torch.float64, device=dev)
+    oh[idx[valid] - 1, torch.nonzero(valid).squeeze(1)] = 1.0
+    # S is [k, p] column-major (k fastest): Tsum[n, m] = sum_{k in n, p in m} S(k|p)
+    Sm = S.view(nm, nm).t()            # Sm[k, p]
+    Tsum = (oh @ Sm @ oh.t()).cpu().numpy()
+    T = np.zeros((nsh, nsh))
+    p2 = F.Plan(ns, 3, 3, "two_thirds", 64, True, ks)
+    Tt = torch.zeros((nsh, nsh), dtype=torch.float64, device=dev)
+    with torch.cuda.stream(stream):
+        p2.shell_to_shell_device(u.data_ptr(), 0, edges, 7, 0, 0, F._lib.S2S_PLAIN, Tt.data_ptr(), 0, 0)
+    torch.cuda.synchronize()
+    T = Tt.cpu().numpy().T            # the library writes T(n, m) column-major
+    scale = np.max(np.abs(T))
+    head = res["fp64_products"]
+    line = {"metric": "32^3 resolved mode-to-mode S(k|p): pairs/s (FP64 sums)", "value": head["pairs_per_s"],
+            "unit": "pairs/s", "n_gpus": 1, "steps": max(1, args.steps), "warmup": 2, "ms_per_step": head["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "32^3 D=3 S(k|p) over all 32768^2 mode pairs, OrszagTwoThirds, E ~ k^4 exp(-2(k/8)^2)",
+                       "seed": args.seed},
+            "forms": res, "shell_sum_vs_shell_to_shell_rel": float(np.max(np.abs(Tsum - T)) / scale),
+            "S_antisymmetry_rel": float((S + S.t()).abs().max().item() / S.abs().max().item()),
+            "net_sum_rel": float(abs(net.sum().item()) / net.abs().sum().item())}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -819,6 +953,10 @@ def main():
         return run_batch(args)
     if args.config == "partial":
         return run_partial(args)
+    if args.config == "padded":
+        return run_padded(args)
+    if args.config == "m2m":
+        return run_m2m(args)
     return run_ours(args)
 
 

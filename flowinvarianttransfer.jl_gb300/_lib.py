@@ -18,7 +18,7 @@ EXPORTS = [
     "fit_mlp_train_grad", "fit_mlp_adam", "fit_gradient_model_flux", "fit_field_moments", "fit_field_compare",
     "fit_batch_create", "fit_batch_destroy", "fit_batch_add_flux", "fit_batch_run", "fit_batch_run_eager", "fit_batch_info",
     "fit_autotune_enable", "fit_autotune_clear", "fit_autotune_info", "fit_autotune_entry",
-    "fit_partial_fluxes_batched",
+    "fit_partial_fluxes_batched", "fit_band_to_band",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -76,6 +76,7 @@ def _declare(lib):
     lib.fit_autotune_clear.argtypes = []
     lib.fit_autotune_info.argtypes = [C.POINTER(i64), C.POINTER(i64), dp, dp]
     lib.fit_autotune_entry.argtypes = [i64, C.POINTER(i64), dp]
+    lib.fit_band_to_band.argtypes = [vp, vp, vp, dp, i32, C.c_double, u32, i32, i32, vp, vp, vp, i32]
     lib.fit_partial_fluxes_batched.argtypes = [vp, vp, i32, C.POINTER(i32), i32, dp, i32, u32, i32, vp, i32]
     lib.fit_mlp_adam.argtypes = [vp, vp, vp, vp, i32, f32, f32, f32, f32, vp]
     for name in EXPORTS:

@@ -13,7 +13,7 @@ import numpy as np
 from . import _lib
 from .plan import get_plan
 from .shells import (coord_is_f32, default_binning, dims_mask, kmax, shell_centers, shell_edges)
-from .types import (DivergentDecomposition, DirectSumBackend, Enstrophy, FFTBackend, GB300Execution,
+from .types import (BandToBandResult, DivergentDecomposition, DirectSumBackend, Enstrophy, FFTBackend, GB300Execution,
                     GB300Spectral, HelicalDecomposition, HelmholtzDecomposition, Helicity, IsotropicShells,
                     KineticEnergy, ModeToModeTransferMethod, ModeToModeTriadResult, NoDecomposition,
                     OrszagTwoThirds, PaddedThreeHalves, PartialFluxResult, PassiveScalar, RotationalDecomposition,
@@ -159,6 +159,20 @@ def calculate_scalar_shell_to_shell_transfer(velocity_hat, scalar_hat, ks, **kw)
     """``calculate_scalar_shell_to_shell_transfer`` (``src/ShellToShell/ShellToShellTransfer.jl:143-147``)."""
     th = _as_component_field(scalar_hat, len(ks))
     return calculate_shell_to_shell_transfer(th, ks, invariant=PassiveScalar(), advecting_hat=velocity_hat, **kw)
+
+
+# ---- smooth band-to-band ----------------------------------------------------------------------------
+def calculate_band_to_band_transfer(velocity_hat, ks, bands, dealiasing=OrszagTwoThirds(), invariant=KineticEnergy(),
+                                    spectral=GB300Spectral(), advecting_hat=None, geometry=IsotropicShells()):
+    """``calculate_band_to_band_transfer`` (``src/BandTransfer.jl:71-113``): smooth T(n,m) between
+    the log-Gaussian ``SmoothBands``; returns centers, transfer_matrix, net_transfer,
+    max_antisymmetry_error."""
+    v = np.asarray(velocity_hat)
+    ft = _ft(v)
+    p = _plan(v, ks, dealiasing, spectral, advecting_hat)
+    T, net, asym = p.band_to_band(v, bands.centers, bands.logwidth, dims_mask(geometry, len(ks)), coord_is_f32(ks),
+                                  invariant.code, advecting_hat)
+    return BandToBandResult(np.asarray(bands.centers, dtype=ft), T.astype(ft), net.astype(ft), ft(asym))
 
 
 # ---- partial fluxes --------------------------------------------------------------------------------

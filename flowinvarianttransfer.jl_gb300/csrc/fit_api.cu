@@ -136,7 +136,7 @@ int ensure_shells(fit_plan* p, const double* edges, int n_edges, unsigned dims, 
 // N̂ half spectrum (M fields) into p->nh. band > 0 restricts the advected field to that shell
 // (the shell-to-shell mediator); reuse_u keeps the advecting velocity from the previous call.
 template <typename T>
-int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u) {
+int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u, int wband) {
   typedef typename Vec2<T>::t V;
   const GridDesc& g = p->g;
   const int nd = p->nd, M = p->M;
@@ -165,8 +165,10 @@ int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, 
     FIT_TRY(inverse_nd<T>(hs, ph, g, p->ax, nfu, inv_m, p->stream));
   }
   a.nfields = (int)nfg;
+  a.wtab = p->wtab.p;
+  a.w_f64 = p->prec == 64;
   for (int c = 0; c < M; ++c)
-    for (int j = 0; j < nd; ++j) a.f[c * nd + j] = GatherField{0, c, j, band};
+    for (int j = 0; j < nd; ++j) a.f[c * nd + j] = GatherField{0, c, j, band, 0, wband};
   FIT_TRY(gather_half<T>(g, p->kt, a, hs + nfu * g.Mhalf, p->stream));
   FIT_TRY(inverse_nd<T>(hs + nfu * g.Mhalf, ph + nfu * g.Mtot, g, p->ax, nfg, inv_m, p->stream));
   FIT_TRY(product<T>(ph, ph + nfu * g.Mtot, (T*)p->nph.p, nd, M, g.Mtot, p->stream));
@@ -175,8 +177,8 @@ int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, 
   return FIT_OK;
 }
 
-template int nonlinear_half<float>(fit_plan*, const void*, const void*, int, bool);
-template int nonlinear_half<double>(fit_plan*, const void*, const void*, int, bool);
+template int nonlinear_half<float>(fit_plan*, const void*, const void*, int, bool, int);
+template int nonlinear_half<double>(fit_plan*, const void*, const void*, int, bool, int);
 
 }  // namespace fit
 
@@ -379,7 +381,7 @@ int fit_plan_destroy(fit_plan* p) {
   s2s_free(p);
   partial_free(p);
   fit_dbuf* bufs[] = {&p->in_u, &p->in_a, &p->in_c, &p->out_c, &p->out_c2, &p->hs, &p->ph, &p->nph, &p->nh,
-                      &p->ceff, &p->seff, &p->partial, &p->outd, &p->shell_full, &p->edges_dev};
+                      &p->ceff, &p->seff, &p->partial, &p->outd, &p->shell_full, &p->edges_dev, &p->wtab};
   for (fit_dbuf* b : bufs) release(b);
   for (int d = 0; d < 3; ++d) {
     if (p->ax_init[d]) axis_free(&p->ax[d]);

@@ -92,6 +92,13 @@ __global__ void __launch_bounds__(256) k_gather(GridDesc g, KTab kt, GatherArgs 
         vx *= G[s];
         vy *= G[s];
       }
+      if (fd.wband > 0) {   // both conjugate modes share |k|, hence the weight of half mode i
+        const long wi = (long)(fd.wband - 1) * g.Mhalf + i;
+        const CT w = a.w_f64 ? (CT) reinterpret_cast<const double*>(a.wtab)[wi]
+                             : (CT) reinterpret_cast<const float*>(a.wtab)[wi];
+        vx *= w;
+        vy *= w;
+      }
       ax += vx;
       ay += s == 1 ? -vy : vy;
     }

@@ -62,6 +62,7 @@ struct GatherField {
   int deriv;   // derivative axis or -1
   int band;    // 1-based shell restriction, 0 = none
   int filt;    // 1: multiply by the filter response G(|k|, ell) of GatherArgs
+  int wband;   // 1-based smooth band: multiply by its weight from GatherArgs::wtab, 0 = none
 };
 struct GatherArgs {
   const void* src[2];
@@ -74,6 +75,8 @@ struct GatherArgs {
   double scale;
   int filter_kind;   // 0 sharp, 1 Gaussian, 2 top-hat (src/Filters.jl:19-26)
   double ell;        // filter scale
+  const void* wtab;  // smooth-band weights on the transform grid's half spectrum, [band][Mhalf]
+  int w_f64;         // wtab element type: 1 double, 0 float
 };
 
 // Spectral filter response G(k, ell) (src/Filters.jl:19-26): sharp 1[|k| < pi/ell], Gaussian

@@ -44,13 +44,17 @@ struct fit_plan {
   void* s2s = nullptr;
   // batched partial-flux state (fit_partial.cu)
   void* partial_state = nullptr;
+  // smooth-band weights on the transform grid's half spectrum (fit_band.cu)
+  fit_dbuf wtab;
+  std::vector<double> wtab_key;
 };
 
 namespace fit {
 int ensure(fit_plan* p, fit_dbuf* b, size_t bytes);
 int ensure_shells(fit_plan* p, const double* edges, int n_edges, unsigned dims, int coord_f32);
+// wband > 0: the advected field is multiplied by smooth-band weight wband of p->wtab instead.
 template <typename T>
-int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u);
+int nonlinear_half(fit_plan* p, const void* f_dev, const void* a_dev, int band, bool reuse_u, int wband = 0);
 // Effective carrier + shell map of the plan's transform grid, and shell sums of a half-spectrum
 // product against it (fit_api.cu).
 template <typename T>

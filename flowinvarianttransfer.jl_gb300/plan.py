@@ -122,6 +122,20 @@ class Plan:
                                               self._vp(asym), PTR_HOST))
         return T, net, float(asym[0])
 
+    def band_to_band(self, u_hat, centers, logwidth, dmask, coord_f32, inv, adv_hat=None):
+        u = self._field(u_hat, self.M)
+        a = None if adv_hat is None else self._field(adv_hat, self.D)
+        c = np.ascontiguousarray(centers, dtype=np.float64)
+        nb = len(c)
+        T = np.zeros((nb, nb), order="F")
+        net = np.zeros(nb)
+        asym = np.zeros(1)
+        with self.lock:
+            check(self.lib.fit_band_to_band(self.h, self._vp(u), self._vp(a), _dptr(c), nb, float(logwidth), dmask,
+                                            int(coord_f32), inv, self._vp(T), self._vp(net), self._vp(asym),
+                                            PTR_HOST))
+        return T, net, float(asym[0])
+
     def helical(self, u_hat):
         u = self._field(u_hat, self.M)
         up = np.empty(self.ns + (3,), dtype=self.cdtype, order="F")
@@ -224,6 +238,10 @@ class Plan:
                                           C.c_void_p(net_ptr) if net_ptr else None,
                                           C.c_void_p(asym_ptr) if asym_ptr else None, PTR_DEVICE))
 
+
+    def mode_to_mode_device(self, u_ptr, inv, fp64, S_ptr, net_ptr):
+        check(self.lib.fit_mode_to_mode(self.h, C.c_void_p(u_ptr), None, inv, int(fp64), C.c_void_p(S_ptr),
+                                        C.c_void_p(net_ptr), PTR_DEVICE))
 
     def coarse_graining_flux_device(self, u_ptr, ell, filter_code, Pi_ptr, A_ptr=0, tau_ptr=0):
         mean = C.c_double()

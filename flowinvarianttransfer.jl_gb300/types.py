@@ -43,6 +43,17 @@ class CustomBinning(AbstractShellBinning):
         object.__setattr__(self, "edges", tuple(float(e) for e in edges))
 
 
+@dataclass(frozen=True)
+class SmoothBands:
+    """Graded log-Gaussian bands (``src/Types.jl:414-430``): centers > 0 increasing, logwidth in ln k."""
+    centers: Tuple[float, ...]
+    logwidth: float = 0.6
+
+    def __init__(self, centers, logwidth=0.6):
+        object.__setattr__(self, "centers", tuple(float(c) for c in centers))
+        object.__setattr__(self, "logwidth", float(logwidth))
+
+
 # ---- shell geometry -----------------------------------------------------------------------------
 @dataclass(frozen=True)
 class ShellMagnitude:
@@ -247,3 +258,12 @@ class CoarseGrainingFluxResultWithDiagnostics:
     mean_flux: float
     tau: np.ndarray
     strain: np.ndarray
+
+
+@dataclass
+class BandToBandResult:
+    """The NamedTuple of ``calculate_band_to_band_transfer`` (``src/BandTransfer.jl:109-111``)."""
+    centers: np.ndarray
+    transfer_matrix: np.ndarray
+    net_transfer: np.ndarray
+    max_antisymmetry_error: float

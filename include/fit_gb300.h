@@ -164,6 +164,16 @@ int fit_forward_spectrum(fit_plan* plan, const void* u_phys, void* u_hat, int pt
 int fit_ns_evolve(fit_plan* plan, void* u_hat, int nsteps, double dt, double nu, double kf, double power,
                   int ptr_kind);
 
+/* Smooth band-to-band transfer T(n,m) between log-Gaussian bands (partition of unity of
+ * exp(-(ln(kappa/centers[n]))^2 / (2 logwidth^2)) over the shell coordinate kappa of dims_mask).
+ * Replaces calculate_band_to_band_transfer (src/BandTransfer.jl:71-113): one nonlinear term per
+ * band m of w_m * u_hat advected by adv_hat (NULL = u_hat), its transfer density against u_hat,
+ * weighted by w_n. T_colmajor[n + nb*m] (nb*nb doubles), net[n] = sum_m T(n,m), max_asym =
+ * max |T(n,m) + T(m,n)|. 1..16 bands. */
+int fit_band_to_band(fit_plan* plan, const void* u_hat, const void* adv_hat, const double* centers, int n_bands,
+                     double logwidth, uint32_t dims_mask, int coord_f32, int invariant, double* T_colmajor,
+                     double* net, double* max_asym, int ptr_kind);
+
 /* ---- uneven batches and the transform autotuner --------------------------------------------------
  * A batch runs many spectral-flux instances, each calculate_spectral_flux / calculate_scalar_flux
  * (src/SpectralFlux.jl:49-94,148-180,203-269) on its own plan (grid, dimension, invariant, shell

@@ -53,6 +53,7 @@ __all__ = [
     "helical_decompose", "toroidal_poloidal_decompose", "helmholtz_decompose", "partial_fluxes",
     "mode_to_mode", "mode_to_mode_triad", "default_binning", "filter_response",
     "coarse_graining_flux", "shell_setup", "set_fft_workers", "s2s_setup", "s2s_column",
+    "band_weights", "band_to_band",
 ]
 
 
@@ -654,3 +655,46 @@ def coarse_graining_flux(u_phys, ks, ell, kind="gaussian"):
             Sij = 0.5 * (grad[i][j] + grad[j][i])
             Pi = Pi - tau * Sij
     return Pi
+
+
+# ---------------------------------------------------------------------------------------------
+# Smooth band-to-band transfer
+# ---------------------------------------------------------------------------------------------
+
+def band_weights(centers, logwidth, kcoord):
+    """Renormalised log-Gaussian band weights ``w_n(kappa)`` (``src/BandTransfer.jl:24-46``):
+    ``exp(-(ln(kappa/c_n))^2 / (2 sigma^2))`` divided by their sum over bands; zero where
+    ``kappa <= 0``."""
+    kappa = np.asarray(kcoord, dtype=np.float64)
+    pos = kappa > 0
+    W = []
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lk = np.log(np.where(pos, kappa, 1.0))
+        for c in centers:
+            r = lk - np.log(float(c))
+            W.append(np.where(pos, np.exp(-(r * r) / (2.0 * logwidth * logwidth)), 0.0))
+    W = np.stack(W)
+    s = W.sum(axis=0)
+    return np.where(s > 0, W / np.where(s > 0, s, 1.0), 0.0)
+
+
+def band_to_band(u_hat, ks, centers, logwidth=0.6, dealiasing="two_thirds", invariant="ke", adv_hat=None,
+                 dims=None):
+    """(centers, T, net, max_asym). Restates ``calculate_band_to_band_transfer``
+    (``src/BandTransfer.jl:71-113``): for each band m the nonlinear term of ``w_m * f`` advected by
+    the full velocity, its transfer density against the full field, weighted by ``w_n``."""
+    nd = len(ks)
+    ns = u_hat.shape[:nd]
+    adv = u_hat if adv_hat is None else adv_hat
+    W = band_weights(centers, logwidth, shell_coordinate(ks, dims))
+    nb = len(centers)
+    T = np.zeros((nb, nb))
+    for m in range(nb):
+        fm = u_hat * W[m][..., None]
+        Nh = nonlinear_term(fm, ks, dealiasing, adv)
+        d = transfer_density(invariant, u_hat, Nh, ks)
+        for n in range(nb):
+            T[n, m] = float(np.sum(W[n] * d))
+    net = T.sum(axis=1)
+    asym = float(np.max(np.abs(T + T.T)))
+    return np.asarray(centers, dtype=np.float64), T, net, asym

@@ -1,0 +1,68 @@
+"""Smooth band-to-band transfer T(K,Q) (src/BandTransfer.jl:71-113) on the GPU against the oracle,
+plus the relational properties the reference tests (test/runtests.jl:661-679)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from fields import curl_noise_3d, scalar_2d, solenoidal_2d
+
+import fit_gb300 as F
+
+
+def test_oracle_band_properties():
+    """The reference's own test case on the oracle: antisymmetric, conserves, reduces."""
+    u, ks = solenoidal_2d(16, 71)
+    _, T, net, asym = O.band_to_band(u, ks, [1.0, 2.0, 3.0, 4.0], 0.5)
+    Tn = np.sqrt(np.sum(T ** 2))
+    assert Tn > 0 and asym < 1e-10 * Tn and abs(T.sum()) < 1e-10 * Tn
+    assert np.allclose(net, T.sum(axis=1), atol=1e-12 * Tn) and abs(net.sum()) < 1e-10 * Tn
+    W = O.band_weights([1.0, 2.0, 3.0, 4.0], 0.5, O.shell_coordinate(ks))
+    kappa = O.shell_coordinate(ks)
+    assert np.allclose(W.sum(axis=0)[kappa > 0], 1.0) and np.all(W[:, kappa == 0] == 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [(64, 1e-11), (32, 2e-5)])
+def test_band_2d_matches_oracle(prec, tol):
+    u, ks = solenoidal_2d(16, 71)
+    bands = F.SmoothBands([1.0, 2.0, 3.0, 4.0], logwidth=0.5)
+    r = F.calculate_band_to_band_transfer(u, ks, bands, spectral=F.GB300Spectral(prec))
+    _, T, net, asym = O.band_to_band(u, ks, [1.0, 2.0, 3.0, 4.0], 0.5)
+    Tn = np.sqrt(np.sum(T ** 2))
+    assert np.max(np.abs(r.transfer_matrix - T)) <= tol * Tn
+    assert np.max(np.abs(r.net_transfer - net)) <= tol * Tn
+    assert r.max_antisymmetry_error <= max(tol, 1e-10) * Tn
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deal", ["two_thirds", "three_halves", "none"])
+def test_band_3d_helicity_and_geometry(deal):
+    u, ks = curl_noise_3d(12, 7)
+    DEAL = {"two_thirds": F.OrszagTwoThirds(), "three_halves": F.PaddedThreeHalves(), "none": F.NoDealiasing()}
+    centers = [1.5, 3.0, 6.0]
+    for inv, oinv, geo, dims in ((F.KineticEnergy(), "ke", F.IsotropicShells(), None),
+                                 (F.Helicity(), "helicity", F.PerpendicularShells(), (1, 2))):
+        r = F.calculate_band_to_band_transfer(u, ks, F.SmoothBands(centers, 0.6), dealiasing=DEAL[deal],
+                                              invariant=inv, spectral=F.GB300Spectral(64), geometry=geo)
+        _, T, net, _ = O.band_to_band(u, ks, centers, 0.6, deal, oinv, dims=dims)
+        Tn = np.sqrt(np.sum(T ** 2))
+        assert np.max(np.abs(r.transfer_matrix - T)) <= 1e-11 * Tn, (deal, oinv)
+
+
+@pytest.mark.gpu
+def test_band_arguments_rejected():
+    u, ks = solenoidal_2d(8, 1)
+    for bands in (F.SmoothBands([2.0, 1.0]), F.SmoothBands([1.0, 2.0], logwidth=0.0), F.SmoothBands([0.0, 1.0]),
+                  F.SmoothBands(np.arange(1.0, 18.0))):
+        with pytest.raises(ValueError):
+            F.calculate_band_to_band_transfer(u, ks, bands, spectral=F.GB300Spectral(64))
+
+
+@pytest.mark.gpu
+def test_band_scalar():
+    u, ks = solenoidal_2d(16, 3)
+    th = scalar_2d(16, 4)
+    r = F.calculate_band_to_band_transfer(th, ks, F.SmoothBands([1.0, 2.5, 5.0], 0.5), invariant=F.PassiveScalar(),
+                                          advecting_hat=u, spectral=F.GB300Spectral(64))
+    _, T, _, _ = O.band_to_band(th, ks, [1.0, 2.5, 5.0], 0.5, "two_thirds", "scalar", adv_hat=u)
+    assert np.max(np.abs(r.transfer_matrix - T)) <= 1e-11 * np.sqrt(np.sum(T ** 2))
