@@ -340,6 +340,8 @@ struct CtTile {
   static constexpr int EPT = E <= 8192 ? 8 : 16;
   static constexpr int NTHR = (E / EPT + 31) / 32 * 32;
   static constexpr size_t SMEM = (size_t)(E + N) * VB;
+  // resident blocks per SM the register budget is sized for (2048 threads per SM)
+  static constexpr int MINB = NTHR >= 768 ? 2 : (NTHR >= 512 ? 3 : 4);
 };
 
 template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS>

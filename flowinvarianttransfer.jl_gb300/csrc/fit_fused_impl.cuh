@@ -35,6 +35,7 @@ struct FzArgs {
   int nsh;
   int nb;       // mediators in this launch
   int med[16];  // their shell numbers (1-based)
+  short ext[16][3];   // per mediator: largest |signed frequency| of its shell's modes along x, y, z
   float sp;     // 1 / Mtot (physical-space normalisation of the inverse transforms)
   float so;     // output normalisation of the forward transform (1/Ntot, or Mtot/Ntot^2 padded)
 };
@@ -44,7 +45,7 @@ FIT_D float2 fz_muli(float2 h, float k) { return make_float2(-h.y * k, h.x * k);
 
 // ---- zinv --------------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zinv(FzArgs a, const float2* __restrict__ H,
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_zinv(FzArgs a, const float2* __restrict__ H,
                                                                     const uint16_t* __restrict__ sb,
                                                                     const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
@@ -58,6 +59,17 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zinv(FzArgs a, c
   const long c0 = (long)blockIdx.z * C;
   const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
   const int m = a.med[b];
+  const int ex = a.ext[b][0], ey = a.ext[b][1], ez = a.ext[b][2];
+  // pencils (kx, ky) outside the mediator's extent hold no mode of its shell: skip the tile (its
+  // outputs are never read: yinv and xmix mask with the same extents)
+  bool live = false;
+  for (int cc = 0; cc < C && !live; ++cc) {
+    const long col = c0 + cc;
+    if (col >= a.P1) break;
+    const int kx = (int)(col % a.KX), ky = (int)(col / a.KX) - a.K;
+    live = kx <= ex && ky >= -ey && ky <= ey;
+  }
+  if (!live) return;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
   const long ob = (((long)b * 3 + c) * 2 + v) * N;
@@ -67,7 +79,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zinv(FzArgs a, c
         const long col = c0 + cc;
         const int f = fz_freq(e, N);
         float2 val = make_float2(0.f, 0.f);
-        if (col < a.P1 && f >= -a.K && f <= a.K) {
+        if (col < a.P1 && f >= -ez && f <= ez) {
           const int kz = f + a.K;
           if (sb[(long)kz * a.P1 + col] == m) {
             val = H[((long)c * a.KY + kz) * a.P1 + col];
@@ -84,7 +96,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zinv(FzArgs a, c
 
 // ---- yinv --------------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yinv(FzArgs a, const float2* __restrict__ in,
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_yinv(FzArgs a, const float2* __restrict__ in,
                                                                     const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
@@ -98,6 +110,8 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yinv(FzArgs a, c
   const int z = blockIdx.z / nkt, k0 = (blockIdx.z % nkt) * C;
   const int c = blockIdx.y / 3, j = blockIdx.y % 3, b = blockIdx.x;
   const int v = (j == 2) ? 1 : 0;
+  const int ex = a.ext[b][0], ey = a.ext[b][1];
+  if (k0 > ex) return;   // no mode of the mediator's shell at these kx (outputs never read)
   const long ib = ((((long)b * 3 + c) * 2 + v) * N + z) * a.P1;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
@@ -108,7 +122,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yinv(FzArgs a, c
         const int kx = k0 + cc;
         const int f = fz_freq(e, N);
         float2 val = make_float2(0.f, 0.f);
-        if (kx < a.KX && f >= -a.K && f <= a.K) {
+        if (kx <= ex && f >= -ey && f <= ey) {
           const int ky = f + a.K;
           val = in[ib + kx + (long)a.KX * ky];
           if (j == 1) val = fz_muli(val, kd[ky]);
@@ -137,6 +151,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_xmix(FzArgs a, c
   const int tid = threadIdx.x;
   const long l0 = (long)blockIdx.z * 2 * C;
   const int b = blockIdx.x;
+  const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
   const long Mtot = (long)N * N * N;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   for (int c = 0; c < 3; ++c) {
@@ -154,7 +169,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_xmix(FzArgs a, c
         const bool cj = 2 * k > N;
         const int kk = cj ? N - k : k;
         float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
-        if (kk <= a.K) {
+        if (kk <= ex) {
           if (la < a.L) A = G[(gb + la) * a.KX + kk];
           if (lb < a.L) B = G[(gb + lb) * a.KX + kk];
           if (j == 0) {
@@ -240,6 +255,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
   const int tid = threadIdx.x;
   const long l0 = (long)blockIdx.z * 2 * C;
   const int b = blockIdx.x;
+  const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
   const long Mtot = (long)N * N * N;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
@@ -291,7 +307,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
           const bool cj = 2 * k > N;
           const int kk = cj ? N - k : k;
           float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
-          if (kk <= a.K) {
+          if (kk <= ex) {
             A = sg[(2 * col) * a.KX + kk];
             B = sg[(2 * col + 1) * a.KX + kk];
             if (j == 0) {
@@ -341,7 +357,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
 
 // ---- yfwd --------------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
   typedef CtTile<float2, N> TT;
@@ -377,7 +393,7 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_yfwd(FzArgs a, c
 // rarely, so each thread keeps a running (shell, sum) pair and flushes it to the block's FP64
 // shared-memory bins only when the shell changes.
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
+__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
                                                                         const float2* __restrict__ Ceff,
                                                                         const uint16_t* __restrict__ seff,
                                                                         double* __restrict__ partial,

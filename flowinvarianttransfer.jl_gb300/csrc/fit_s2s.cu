@@ -33,6 +33,7 @@ struct S2SState {
   long key_gen = -1;
   const double* key_T = nullptr;
   std::vector<int> occ;   // retained modes per shell
+  std::vector<int> ext;   // per shell: largest |signed frequency| along x, y, z
   fit_dbuf occ_dev;
   // fused-path buffers
   fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr;
@@ -50,24 +51,43 @@ void s2s_free(fit_plan* p) {
   p->s2s = nullptr;
 }
 
-__global__ void k_occupancy(GridDesc g, const uint16_t* __restrict__ sh, int two_thirds, int* occ) {
-  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= g.Ntot) return;
-  const int s = sh[i];
-  if (!s) return;
-  if (two_thirds) {
+// Per shell: retained modes (occ) and the largest |signed frequency| of its modes along each axis
+// (ext, 3 per shell), block-local in shared memory and flushed with one atomic per shell touched.
+__global__ void k_shell_stats(GridDesc g, const uint16_t* __restrict__ sh, int two_thirds, int nsh, int* occ,
+                              int* ext) {
+  extern __shared__ int st[];   // occ[nsh], ext[3 nsh]
+  for (int t = threadIdx.x; t < 4 * nsh; t += blockDim.x) st[t] = 0;
+  __syncthreads();
+  const long step = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < g.Ntot; i += step) {
+    const int s = sh[i];
+    if (!s) continue;
     int k[3];
-    k[0] = (int)(i % g.N[0]);
-    const long r = i / g.N[0];
-    k[1] = (int)(r % g.N[1]);
-    k[2] = (int)(r / g.N[1]);
-    for (int d = 0; d < g.nd; ++d) {
-      const int N = g.N[d];
-      const int a = (k[d] <= N / 2) ? k[d] : N - k[d];
-      if (a >= N / 3) return;
+    decode_full(g, i, k);
+    bool keep = true;
+    int f[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d < g.nd) {
+        const int N = g.N[d];
+        const int a = (k[d] <= N / 2) ? k[d] : N - k[d];
+        if (two_thirds && a >= N / 3) keep = false;
+        f[d] = (2 * k[d] < N) ? k[d] : N - k[d];   // |signed frequency|, index N/2 -> N/2
+      }
+    }
+    if (!keep) continue;
+    atomicAdd(&st[s - 1], 1);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) atomicMax(&st[nsh + 3 * (s - 1) + d], f[d]);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nsh; t += blockDim.x) {
+    if (st[t]) {
+      atomicAdd(&occ[t], st[t]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) atomicMax(&ext[3 * t + d], st[nsh + 3 * t + d]);
     }
   }
-  atomicAdd(&occ[s - 1], 1);
 }
 
 template <typename T>
@@ -297,7 +317,13 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   const float2* tw = p->ax[0].tw32;
   for (size_t b0 = 0; b0 < meds.size(); b0 += B) {
     a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
-    for (int b = 0; b < a.nb; ++b) a.med[b] = meds[b0 + b];
+    for (int b = 0; b < a.nb; ++b) {
+      a.med[b] = meds[b0 + b];
+      for (int d = 0; d < 3; ++d) {   // the mediator's extent in live-box units (never beyond K)
+        const int e = s->ext[3 * (a.med[b] - 1) + d];
+        a.ext[b][d] = (short)(e < K ? e : K);
+      }
+    }
     int rc = fz_dispatch_a(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
                            (float2*)s->fB.p, (double*)s->fpart.p, tw, (int*)s->ferr.p, p->stream);
     if (rc == 1)
@@ -348,15 +374,27 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
   if (!same) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
     s->exec = nullptr;
-    // retained-mode occupancy of every shell
-    FIT_TRY(ensure(p, &s->occ_dev, sizeof(int) * p->nsh));
-    FIT_CUDA_CHECK(cudaMemsetAsync(s->occ_dev.p, 0, sizeof(int) * p->nsh, p->stream));
-    k_occupancy<<<(unsigned)((p->g.Ntot + 255) / 256), 256, 0, p->stream>>>(
-        p->g, (const uint16_t*)p->shell_full.p, p->dealias == 1, (int*)s->occ_dev.p);
+    // retained-mode occupancy and per-axis extent of every shell
+    const int nsh = p->nsh;
+    const size_t smem = sizeof(int) * 4 * (size_t)nsh;
+    if (smem > 200 * 1024) {
+      fit_set_error("too many shells (%d) for the batched shell-to-shell form", nsh);
+      return FIT_ERR_SIZE;
+    }
+    if (smem > 48 * 1024)
+      FIT_CUDA_CHECK(cudaFuncSetAttribute(k_shell_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FIT_TRY(ensure(p, &s->occ_dev, sizeof(int) * 4 * nsh));
+    FIT_CUDA_CHECK(cudaMemsetAsync(s->occ_dev.p, 0, sizeof(int) * 4 * nsh, p->stream));
+    long blocks = (p->g.Ntot + 255) / 256;
+    if (blocks > 4 * 152) blocks = 4 * 152;
+    k_shell_stats<<<(unsigned)blocks, 256, smem, p->stream>>>(p->g, (const uint16_t*)p->shell_full.p, p->dealias == 1,
+                                                           nsh, (int*)s->occ_dev.p, (int*)s->occ_dev.p + nsh);
     FIT_LAUNCH_CHECK();
-    s->occ.assign(p->nsh, 0);
-    FIT_CUDA_CHECK(cudaMemcpyAsync(s->occ.data(), s->occ_dev.p, sizeof(int) * p->nsh, cudaMemcpyDeviceToHost, p->stream));
+    std::vector<int> h(4 * (size_t)nsh);
+    FIT_CUDA_CHECK(cudaMemcpyAsync(h.data(), s->occ_dev.p, sizeof(int) * 4 * nsh, cudaMemcpyDeviceToHost, p->stream));
     FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));
+    s->occ.assign(h.begin(), h.begin() + nsh);
+    s->ext.assign(h.begin() + nsh, h.end());
     // first call for this key: run eagerly (allocates the workspace, sets kernel attributes)
     const int rc = run_s2s(p, s, ud, ad, inv, Td);
     if (rc != FIT_OK) return rc;
