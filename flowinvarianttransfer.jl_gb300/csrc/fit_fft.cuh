@@ -598,4 +598,76 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
   }
 }
 
+// ct_fft_mapped with a hook between the inner stages and the last one: mid() runs on every thread
+// (it may synchronise the block) and returns false to abandon the transform (then store is never
+// called). Used where the last stage's consumer needs data that arrives while the transform runs.
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, typename LD, typename MID, typename ST>
+__device__ __forceinline__ bool ct_fft_mapped_mid(V* s, const V* tw, int tid, LD load, MID mid, ST store) {
+  typedef CtMap<N> MP;
+  constexpr int RL = MP::RL, NRL = MP::NRL;
+  constexpr int MB = (EPT + RL - 1) / RL;
+  constexpr int NB = C * NRL;
+  V v[MB][RL];
+  if constexpr (MP::DIRECT) {
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) v[i][q] = load(i, q, j + q * NRL, c);
+        dftr<V, RL, INV>(v[i]);
+#pragma unroll
+        for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+      }
+    }
+    __syncthreads();
+    ct_stages_range<V, INV, N, C, NTHR, EPT, 1, MP::NST - 1>(s, tw, tid);
+    if (!mid()) return false;
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) {
+          V x = s[swz(j + q * NRL, c, C)];
+          if (q > 0) {
+            V w = tw[j * q];
+            if (INV) w.y = -w.y;
+            x = cmul(x, w);
+          }
+          v[i][q] = x;
+        }
+        dftr<V, RL, INV>(v[i]);
+#pragma unroll
+        for (int q = 0; q < RL; ++q) store(i, q, j + q * NRL, c, v[i][q]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) s[swz(j + q * NRL, c, C)] = load(i, q, j + q * NRL, c);
+      }
+    }
+    __syncthreads();
+    ct_stages<V, INV, N, C, NTHR, EPT, 0>(s, tw, tid);
+    if (!mid()) return false;
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int b = tid + i * NTHR;
+      if (NB % NTHR == 0 || b < NB) {
+        const int c = b % C, j = b / C;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) store(i, q, j + q * NRL, c, s[swz(j + q * NRL, c, C)]);
+      }
+    }
+  }
+  return true;
+}
+
 }  // namespace fit

@@ -22,6 +22,8 @@
 //   xmix out  [b][c][line = y + N z][kx]   yfwd out [b][c][z][ky'][kx]
 #pragma once
 
+#include <stdlib.h>
+
 #include "fit_fft.cuh"
 #include "fit_maps.cuh"
 #include "fit_tma.cuh"
@@ -297,7 +299,12 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
     }
     const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL);
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicExch(err, 1);
+      if (tid == 0) {
+        atomicExch(err, 1);
+        // bounded chance for this tile and the prefetched next one to land before the block exits
+        mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 200000000LL);
+        if (t + 1 < 9) mbar_wait_bounded(&bar[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1), 200000000LL);
+      }
       return;
     }
     const float2* sg = stg + buf * SB;
@@ -340,6 +347,164 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
       }
       __syncthreads();
       ct_stages<float2, false, N, C, NT, EPT, 0>(s, tw, tid);
+      const long obase = ((long)b * 3 + c) * a.L;
+      const float hs = 0.5f * a.so;
+      for (int i = tid; i < C * a.KX; i += NT) {
+        const int col = i / a.KX, k = i % a.KX;
+        const long la = l0 + 2 * col, lb = la + 1;
+        const float2 zk = s[swz(k, col, C)];
+        const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
+        out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+        out[(obase + lb) * a.KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---- xmix, register-accumulating form -------------------------------------------------------------
+// Same arithmetic as k_fz_xmix_bulk, restructured so that no transform output makes an extra round
+// trip through shared memory: the advecting-velocity tile of the current j (2C lines x N floats,
+// contiguous in U) is bulk-copied into shared memory, the inverse transform's last stage hands its
+// outputs (butterfly order) to a store that accumulates u_j * value straight into registers, and
+// the forward transform's first stage reads those registers (the element map of a transform's last
+// stage is the map of the next transform's first stage). Gradient tiles are double-buffered as in
+// k_fz_xmix_bulk; the single velocity buffer is refilled after each step's final barrier and waited
+// for only before the last stage of the next inverse transform, so its copy overlaps two stages.
+template <int N>
+struct XRTile {
+  static constexpr int C = XTile<N>::C;
+  static constexpr int E = C * N;
+  static constexpr int EPT = XTile<N>::EPT;
+  static constexpr int NTHR = XTile<N>::NTHR;
+  // velocity tile rows padded to N + 4 floats (16-byte aligned rows): the butterfly-order reads of
+  // the 8 columns of a warp then fall on distinct banks in pairs instead of all on one bank
+  static constexpr int UP = N + 4;
+  static constexpr size_t U_BYTES = (size_t)2 * C * UP * 4;
+  // s, twiddles, 3 mbarriers, then the velocity tile, then two gradient staging buffers
+  static constexpr size_t OFF_U = (((size_t)(E + N) * 8 + 32) + 127) / 128 * 128;
+  static constexpr size_t OFF_G = OFF_U + U_BYTES;
+  // the register accumulators need the last stage's radix to divide the elements per thread
+  static constexpr bool OK = EPT % CtMap<N>::RL == 0 && NTHR * EPT == E;
+};
+
+template <int N>
+__global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, const float2* __restrict__ G,
+                                                                const float* __restrict__ U,
+                                                                const float* __restrict__ kd,
+                                                                float2* __restrict__ out,
+                                                                const float2* __restrict__ twg, int* err) {
+  typedef XRTile<N> TT;
+  constexpr int C = TT::C, NT = TT::NTHR, EPT = TT::EPT;
+  typedef CtMap<N> MP;
+  constexpr int RL = MP::RL;
+  constexpr int MB = (EPT + RL - 1) / RL;
+  static_assert(MB * RL == EPT && NT * EPT == TT::E, "xmix needs an exact thread/element split");
+  extern __shared__ __align__(128) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + TT::E;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + N);   // [0],[1] gradient buffers, [2] velocity
+  float* us = reinterpret_cast<float*>(fit_smem_raw + TT::OFF_U);
+  float2* stg = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_G);
+  const int SB = 2 * C * a.KX;
+  const uint32_t gbytes = (uint32_t)SB * 8u;
+  const int tid = threadIdx.x;
+  const long l0 = (long)blockIdx.z * 2 * C;
+  const int b = blockIdx.x;
+  const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
+  const long Mtot = (long)N * N * N;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    mbar_init_fence();
+  }
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  if (tid == 0) {
+    const long gb = ((long)b * 3 * 3) * a.L;
+    mbar_expect_tx(&bar[0], gbytes);
+    bulk_g2s(stg, G + (gb + l0) * a.KX, gbytes, &bar[0]);
+    mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
+    for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + r * TT::UP, U + (l0 + r) * N, (uint32_t)(N * 4), &bar[2]);
+  }
+  // after a timed-out wait: give the copies this block still has in flight a bounded chance to
+  // land before the block exits (gradient tiles t and t+1, velocity tile t)
+  auto drain = [&](int t, bool g_done, bool u_done) {
+    if (tid != 0) return;
+    if (!g_done) mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1), 200000000LL);
+    if (t + 1 < 9) mbar_wait_bounded(&bar[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1), 200000000LL);
+    if (!u_done) mbar_wait_bounded(&bar[2], (uint32_t)(t & 1), 200000000LL);
+  };
+  float2 acc[MB][RL];
+  for (int t = 0; t < 9; ++t) {
+    const int c = t / 3, j = t % 3, buf = t & 1;
+    if (j == 0) {
+#pragma unroll
+      for (int i = 0; i < MB; ++i)
+#pragma unroll
+        for (int q = 0; q < RL; ++q) acc[i][q] = make_float2(0.f, 0.f);
+    }
+    if (tid == 0 && t + 1 < 9) {
+      const int c1 = (t + 1) / 3, j1 = (t + 1) % 3, nb1 = (t + 1) & 1;
+      const long gb = (((long)b * 3 + c1) * 3 + j1) * a.L;
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[nb1], gbytes);
+      bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KX, gbytes, &bar[nb1]);
+    }
+    const bool okg = mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL);
+    if (__syncthreads_or(!okg)) {
+      if (tid == 0) atomicExch(err, 1);
+      drain(t, false, false);
+      return;
+    }
+    const float2* sg = stg + buf * SB;
+    const float sp = a.sp;
+    const bool ok = ct_fft_mapped_mid<float2, true, N, C, NT, EPT>(
+        s, tw, tid,
+        [&](int, int, int k, int col) -> float2 {
+          const bool cj = 2 * k > N;
+          const int kk = cj ? N - k : k;
+          float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+          if (kk <= ex) {
+            A = sg[(2 * col) * a.KX + kk];
+            B = sg[(2 * col + 1) * a.KX + kk];
+            if (j == 0) {
+              const float kx = kd[a.K + kk];
+              A = fz_muli(A, kx);
+              B = fz_muli(B, kx);
+            }
+            if (cj) { A.y = -A.y; B.y = -B.y; }
+            if (k == 0) { A.y = 0.f; B.y = 0.f; }
+          }
+          return make_float2(A.x - B.y, A.y + B.x);
+        },
+        [&]() -> bool {   // the velocity tile of this j must have landed before the last stage
+          const bool oku = mbar_wait_bounded(&bar[2], (uint32_t)(t & 1), 2000000000LL);
+          return !__syncthreads_or(!oku);
+        },
+        [&](int i, int q, int x, int col, float2 zv) {
+          acc[i][q].x += us[(2 * col) * TT::UP + x] * (zv.x * sp);
+          acc[i][q].y += us[(2 * col + 1) * TT::UP + x] * (zv.y * sp);
+        });
+    if (!ok) {
+      if (tid == 0) atomicExch(err, 1);
+      drain(t, true, false);
+      return;
+    }
+    __syncthreads();   // s and the velocity tile are free
+    if (tid == 0 && t + 1 < 9) {
+      const int j1 = (t + 1) % 3;
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
+      const float* src = U + (long)j1 * Mtot + l0 * N;
+      for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + r * TT::UP, src + (long)r * N, (uint32_t)(N * 4), &bar[2]);
+    }
+    if (j == 2) {
+      ct_fft_mapped<float2, false, N, C, NT, EPT>(
+          s, tw, tid, [&](int i, int q, int, int) -> float2 { return acc[i][q]; },
+          [&](int, int, int x, int col, float2 val) { s[swz(x, col, C)] = val; });
+      __syncthreads();
       const long obase = ((long)b * 3 + c) * a.L;
       const float hs = 0.5f * a.so;
       for (int i = tid; i < C * a.KX; i += NT) {
@@ -500,7 +665,19 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
     typedef XTile<N> XT;
     const size_t smx = XT::SMEM_FIXED + 2 * (size_t)(2 * XT::C * a.KX) * 8;
     const bool bulk = smx <= 227 * 1024 && (a.L % (2 * XT::C)) == 0;   // 16-byte alignment holds: L, 2C are multiples of 16
-    if (bulk) {
+    typedef XRTile<N> XR;
+    const size_t smr = XR::OFF_G + 2 * (size_t)(2 * XR::C * a.KX) * 8;
+    const char* env = getenv("FIT_XMIX_BULK");   // selects the previous form of the x pass
+    bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
+    if constexpr (XR::OK) {
+      if (reg) {
+        FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr));
+        k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(a, bufB, U, kd, bufA,
+                                                                                             tw, err);
+      }
+    }
+    if (reg) {
+    } else if (bulk) {
       FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx));
       k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, bufB, U, kd, bufA, tw,
                                                                                              err);

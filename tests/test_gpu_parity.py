@@ -226,8 +226,13 @@ def test_zero_field_gives_zero():
 @pytest.mark.parametrize("deal", ["two_thirds", "three_halves"])
 @pytest.mark.parametrize("inv", ["ke", "helicity"])
 @pytest.mark.parametrize("herm", [True, False])
-def test_fused_shell_to_shell_64(deal, inv, herm):
-    """The fused FP32 pipeline (cubic grid of a compiled size) against the FP64 oracle."""
+@pytest.mark.parametrize("xpass", ["register", "staged"])
+def test_fused_shell_to_shell_64(deal, inv, herm, xpass, monkeypatch):
+    """The fused FP32 pipeline (cubic grid of a compiled size) against the FP64 oracle, with both
+    forms of its x pass (register-accumulating and shared-memory staged)."""
+    if xpass == "staged":
+        monkeypatch.setenv("FIT_XMIX_BULK", "1")
+    F.clear_plans()
     if herm:
         u, ks = spectrum_field((64, 64, 64), e_config2, seed=5)
     else:
