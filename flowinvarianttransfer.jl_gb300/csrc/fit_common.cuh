@@ -82,6 +82,27 @@ bool fit_prof_on();
 void fit_prof_begin(int kind, double bytes, cudaStream_t st);
 void fit_prof_end(cudaStream_t st);
 
+// Shared-memory carveout sized for occupancy: the blocks per SM that threads and registers allow,
+// times the block's shared footprint (+1 KB reserved per block), as a percentage of the SM's 228 KB;
+// the rest stays L1. (Leaving the default can cap resident blocks; asking for the maximum shrinks L1
+// for kernels that do not need it.)
+template <typename K>
+inline cudaError_t set_occupancy_carveout(K kern, size_t dyn_smem, int nthr) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+  if (e != cudaSuccess) return e;
+  const int regs = fa.numRegs > 0 ? ((fa.numRegs + 7) / 8) * 8 : 32;
+  int blocks = 2048 / (nthr > 0 ? nthr : 1);
+  const int by_regs = 65536 / (regs * (nthr > 0 ? nthr : 1));
+  if (by_regs < blocks) blocks = by_regs;
+  if (blocks < 1) blocks = 1;
+  const double need = (double)blocks * ((double)dyn_smem + (double)fa.sharedSizeBytes + 1024.0);
+  int pct = (int)(100.0 * need / (228.0 * 1024.0) + 0.999);
+  if (pct > 100) pct = 100;
+  if (pct < 0) pct = 0;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
 // Radix schedule of one transform length (product of the entries = N).
 struct Radices {
   int n;

@@ -14,14 +14,15 @@
 namespace fit {
 
 template <typename K>
-static int ct_prep(K kern, size_t smem) {
+static int ct_prep(K kern, size_t smem, int nthr) {
   static std::mutex mu;
   static std::unordered_map<const void*, size_t> done;
-  if (smem <= 48 * 1024) return FIT_OK;
   std::lock_guard<std::mutex> lk(mu);
   auto it = done.find((const void*)kern);
   if (it != done.end() && it->second >= smem) return FIT_OK;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = set_occupancy_carveout(kern, smem, nthr);
   if (e != cudaSuccess) {
     fit_set_error("cudaFuncSetAttribute(smem=%zu) failed: %s", smem, cudaGetErrorString(e));
     return FIT_ERR_CUDA;
@@ -39,7 +40,7 @@ static int ct_strided_n(const V* in, V* out, long P, long Q, typename Scal<V>::t
     fit_set_error("grid too large");
     return FIT_ERR_SIZE;
   }
-  FIT_TRY(ct_prep(k_ct_strided<V, INV, N>, TT::SMEM));
+  FIT_TRY(ct_prep(k_ct_strided<V, INV, N>, TT::SMEM, TT::NTHR));
   k_ct_strided<V, INV, N><<<(unsigned)grid, TT::NTHR, TT::SMEM, st>>>(in, out, P, tpq, tw, scale);
   return FIT_OK;
 }
@@ -49,7 +50,7 @@ static int ct_c2r_n(const V* in, typename Scal<V>::t* out, long L, typename Scal
                     cudaStream_t st) {
   typedef CtTile<V, N> TT;
   const long grid = (L + 2L * TT::C - 1) / (2L * TT::C);
-  FIT_TRY(ct_prep(k_ct_c2r_x<V, N>, TT::SMEM));
+  FIT_TRY(ct_prep(k_ct_c2r_x<V, N>, TT::SMEM, TT::NTHR));
   k_ct_c2r_x<V, N><<<(unsigned)grid, TT::NTHR, TT::SMEM, st>>>(in, out, L, tw, scale);
   return FIT_OK;
 }
@@ -59,7 +60,7 @@ static int ct_r2c_n(const typename Scal<V>::t* in, V* out, long L, typename Scal
                     cudaStream_t st) {
   typedef CtTile<V, N> TT;
   const long grid = (L + 2L * TT::C - 1) / (2L * TT::C);
-  FIT_TRY(ct_prep(k_ct_r2c_x<V, N>, TT::SMEM));
+  FIT_TRY(ct_prep(k_ct_r2c_x<V, N>, TT::SMEM, TT::NTHR));
   k_ct_r2c_x<V, N><<<(unsigned)grid, TT::NTHR, TT::SMEM, st>>>(in, out, L, tw, scale);
   return FIT_OK;
 }

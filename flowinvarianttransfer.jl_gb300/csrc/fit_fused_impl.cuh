@@ -24,6 +24,9 @@
 
 #include <stdlib.h>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "fit_fft.cuh"
 #include "fit_maps.cuh"
 #include "fit_tma.cuh"
@@ -623,14 +626,22 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MI
   for (int t = tid; t < a.nsh; t += NT) pb[t] = bins[t];
 }
 
+// Raise the dynamic shared-memory limit and size the carveout for the kernel's occupancy.
 template <typename K>
-static int ct_prep_fused(K kern, size_t smem) {
-  if (smem <= 48 * 1024) return FIT_OK;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static int ct_prep_fused(K kern, size_t smem, int nthr) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> done;   // kernels already prepared, by footprint
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = done.find((const void*)kern);
+  if (it != done.end() && it->second >= smem) return FIT_OK;
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = set_occupancy_carveout(kern, smem, nthr);
   if (e != cudaSuccess) {
     fit_set_error("cudaFuncSetAttribute(smem=%zu) failed: %s", smem, cudaGetErrorString(e));
     return FIT_ERR_CUDA;
   }
+  done[(const void*)kern] = smem;
   return FIT_OK;
 }
 
@@ -643,11 +654,11 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   constexpr int C = TT::C;
   const size_t sm = TT::SMEM;
   const size_t smb = TT::SMEM + sizeof(double) * a.nsh + 16;
-  FIT_TRY(ct_prep_fused(k_fz_zinv<N>, sm));
-  FIT_TRY(ct_prep_fused(k_fz_yinv<N>, sm));
-  FIT_TRY(ct_prep_fused(k_fz_xmix<N>, sm));
-  FIT_TRY(ct_prep_fused(k_fz_yfwd<N>, sm));
-  FIT_TRY(ct_prep_fused(k_fz_zfwd_bin<N>, smb));
+  FIT_TRY(ct_prep_fused(k_fz_zinv<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_yinv<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_xmix<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_yfwd<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_zfwd_bin<N>, smb, TT::NTHR));
   const unsigned pt = (unsigned)((a.P1 + C - 1) / C);
   const unsigned nkt = (unsigned)((a.KX + C - 1) / C);
   const double cpx = 8.0;
@@ -671,14 +682,14 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
     bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
     if constexpr (XR::OK) {
       if (reg) {
-        FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr));
+        FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
         k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(a, bufB, U, kd, bufA,
                                                                                              tw, err);
       }
     }
     if (reg) {
     } else if (bulk) {
-      FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx));
+      FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx, XT::NTHR));
       k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, bufB, U, kd, bufA, tw,
                                                                                              err);
     } else {

@@ -130,14 +130,15 @@ static Tile pick_tile(int N, int vbytes, long avail_cols) {
 // Raise the dynamic shared-memory limit of a kernel once (the attribute is per function; a
 // cached value keeps the call out of captured launch sequences after the first use).
 template <typename K>
-static int prep_kernel(K kern, size_t smem) {
+static int prep_kernel(K kern, size_t smem, int nthr) {
   static std::mutex mu;
   static std::unordered_map<const void*, size_t> done;
-  if (smem <= 48 * 1024) return FIT_OK;
   std::lock_guard<std::mutex> lk(mu);
   auto it = done.find((const void*)kern);
   if (it != done.end() && it->second >= smem) return FIT_OK;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = set_occupancy_carveout(kern, smem, nthr);
   if (e != cudaSuccess) {
     fit_set_error("cudaFuncSetAttribute(smem=%zu) failed: %s", smem, cudaGetErrorString(e));
     return FIT_ERR_CUDA;
@@ -230,7 +231,7 @@ static int launch_cand(int kind, const void* in, void* out, const Axis& ax, long
     if (grid > 2147483647L) return 1;
 #define FIT_TS(INV, EPT)                                                                                      \
   do {                                                                                                        \
-    FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, smem));                                                  \
+    FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, smem, (int)nthr));                                                  \
     k_pass_strided<V, INV, EPT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const V*)in, (V*)out, N, P, tpq, \
                                                                                c.C, rd, tw, scale);           \
   } while (0)
@@ -245,18 +246,18 @@ static int launch_cand(int kind, const void* in, void* out, const Axis& ax, long
   const long grid = (P + 2L * c.C - 1) / (2L * c.C);
   if (kind == PASS_C2R) {
     if (c.ept == 8) {
-      FIT_TRY(prep_kernel(k_c2r_x<V, 8>, smem));
+      FIT_TRY(prep_kernel(k_c2r_x<V, 8>, smem, (int)nthr));
       k_c2r_x<V, 8><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const V*)in, (T*)out, N, P, c.C, rd, tw, scale);
     } else {
-      FIT_TRY(prep_kernel(k_c2r_x<V, 16>, smem));
+      FIT_TRY(prep_kernel(k_c2r_x<V, 16>, smem, (int)nthr));
       k_c2r_x<V, 16><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const V*)in, (T*)out, N, P, c.C, rd, tw, scale);
     }
   } else {
     if (c.ept == 8) {
-      FIT_TRY(prep_kernel(k_r2c_x<V, 8>, smem));
+      FIT_TRY(prep_kernel(k_r2c_x<V, 8>, smem, (int)nthr));
       k_r2c_x<V, 8><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const T*)in, (V*)out, N, P, c.C, rd, tw, scale);
     } else {
-      FIT_TRY(prep_kernel(k_r2c_x<V, 16>, smem));
+      FIT_TRY(prep_kernel(k_r2c_x<V, 16>, smem, (int)nthr));
       k_r2c_x<V, 16><<<(unsigned)grid, (unsigned)nthr, smem, st>>>((const T*)in, (V*)out, N, P, c.C, rd, tw, scale);
     }
   }
@@ -442,7 +443,7 @@ int pass_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, const 
   }
 #define FIT_PS_LAUNCH(INV, EPT)                                                                          \
   do {                                                                                                 \
-    FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, t.smem));                                         \
+    FIT_TRY(prep_kernel(k_pass_strided<V, INV, EPT>, t.smem, t.nthr));                                         \
     k_pass_strided<V, INV, EPT><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, P, tpq, t.C, ax.rd, tw, \
                                                                           scale);                      \
   } while (0)
@@ -487,10 +488,10 @@ int pass_c2r_x(const typename Vec2<T>::t* in, T* out, const Axis& ax, long L, T 
     }
   }
   if (t.EPT == 8) {
-    FIT_TRY(prep_kernel(k_c2r_x<V, 8>, t.smem));
+    FIT_TRY(prep_kernel(k_c2r_x<V, 8>, t.smem, t.nthr));
     k_c2r_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
   } else {
-    FIT_TRY(prep_kernel(k_c2r_x<V, 16>, t.smem));
+    FIT_TRY(prep_kernel(k_c2r_x<V, 16>, t.smem, t.nthr));
     k_c2r_x<V, 16><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
   }
   fit_prof_end(st);
@@ -528,10 +529,10 @@ int pass_r2c_x(const T* in, typename Vec2<T>::t* out, const Axis& ax, long L, T 
     }
   }
   if (t.EPT == 8) {
-    FIT_TRY(prep_kernel(k_r2c_x<V, 8>, t.smem));
+    FIT_TRY(prep_kernel(k_r2c_x<V, 8>, t.smem, t.nthr));
     k_r2c_x<V, 8><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
   } else {
-    FIT_TRY(prep_kernel(k_r2c_x<V, 16>, t.smem));
+    FIT_TRY(prep_kernel(k_r2c_x<V, 16>, t.smem, t.nthr));
     k_r2c_x<V, 16><<<(unsigned)grid, t.nthr, t.smem, st>>>(in, out, ax.N, L, t.C, ax.rd, tw, scale);
   }
   fit_prof_end(st);
