@@ -366,6 +366,15 @@ int fit_plan_create(fit_plan** out, int nd, const int64_t* ns, int n_advected, i
       rc = FIT_ERR_CUDA;
     }
     p->kt.k[d] = p->ks_dev[d];
+    std::vector<float> k32(N);
+    for (int i = 0; i < N; ++i) k32[i] = (float)kk[i];
+    if (rc == FIT_OK && (cudaMalloc(&p->ks32_dev[d], sizeof(float) * N) != cudaSuccess ||
+                         cudaMemcpy(p->ks32_dev[d], k32.data(), sizeof(float) * N, cudaMemcpyHostToDevice) !=
+                             cudaSuccess)) {
+      fit_set_error("ks upload failed");
+      rc = FIT_ERR_CUDA;
+    }
+    p->kt.k32[d] = p->ks32_dev[d];
   }
   if (rc != FIT_OK) {
     fit_plan_destroy(p);
@@ -386,6 +395,7 @@ int fit_plan_destroy(fit_plan* p) {
   for (int d = 0; d < 3; ++d) {
     if (p->ax_init[d]) axis_free(&p->ax[d]);
     if (p->ks_dev[d]) cudaFree(p->ks_dev[d]);
+    if (p->ks32_dev[d]) cudaFree(p->ks32_dev[d]);
   }
   if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
   delete p;

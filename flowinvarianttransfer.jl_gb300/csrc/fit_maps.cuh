@@ -131,9 +131,9 @@ FIT_D void carrier_at_t(const GridDesc& g, const KTab& kt, const void* car, int 
       if (c < nc) C[c] = u[c];
     return;
   }
-  const CT kx = (CT)kt.k[0][k[0]];
-  const CT ky = g.nd >= 2 ? (CT)kt.k[1][k[1]] : (CT)0;
-  const CT kz = g.nd >= 3 ? (CT)kt.k[2][k[2]] : (CT)0;
+  const CT kx = ktab_at<CT>(kt, 0, k[0]);
+  const CT ky = g.nd >= 2 ? ktab_at<CT>(kt, 1, k[1]) : (CT)0;
+  const CT kz = g.nd >= 3 ? ktab_at<CT>(kt, 2, k[2]) : (CT)0;
   if (inv == INV_ENSTROPHY && g.nd == 2) {
     // w = i (kx uy - ky ux)
     const C2 w = mkc<C2>(-(kx * u[1].y - ky * u[0].y), kx * u[1].x - ky * u[0].x);

@@ -51,15 +51,17 @@ __global__ void __launch_bounds__(256) k_gather(GridDesc g, KTab kt, GatherArgs 
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     ok[s] = kk[s].lin >= 0 && (!a.two_thirds || keep23(g, kk[s].k));
-    double k2 = 0.0;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const double kv = (d < g.nd && ok[s]) ? kt.k[d][kk[s].k[d]] : 0.0;
-      kd[s][d] = (CT)kv;
-      k2 += kv * kv;
-    }
+    for (int d = 0; d < 3; ++d) kd[s][d] = (d < g.nd && ok[s]) ? ktab_at<CT>(kt, d, kk[s].k[d]) : (CT)0;
     if (ok[s] && any_band) sh[s] = a.shell_full[kk[s].lin];
-    if (ok[s] && any_filt) G[s] = (CT)filter_response(a.filter_kind, sqrt(k2), a.ell);
+    if (ok[s] && any_filt) {   // |k| in FP64 for the filter response
+      double k2 = 0.0;
+      for (int d = 0; d < g.nd; ++d) {
+        const double kv = kt.k[d][kk[s].k[d]];
+        k2 += kv * kv;
+      }
+      G[s] = (CT)filter_response(a.filter_kind, sqrt(k2), a.ell);
+    }
   }
   const CT sc = (CT)(0.5 * a.scale);
 #pragma unroll
@@ -507,7 +509,7 @@ __global__ void __launch_bounds__(256) k_helical(GridDesc g, KTab kt, const void
   if (i >= g.Ntot) return;
   int k[3];
   decode_full(g, i, k);
-  const CT kx = (CT)kt.k[0][k[0]], ky = (CT)kt.k[1][k[1]], kz = (CT)kt.k[2][k[2]];
+  const CT kx = ktab_at<CT>(kt, 0, k[0]), ky = ktab_at<CT>(kt, 1, k[1]), kz = ktab_at<CT>(kt, 2, k[2]);
   const CT kk = sqrt(kx * kx + ky * ky + kz * kz);
   const long n = g.Ntot;
   C2 P[3], Mv[3];

@@ -49,10 +49,21 @@ bool autotune_entry(long i, long* fields, float* ms_best, float* ms_default);
 
 // ---- pointwise / reduction kernels (fit_ops.cu) ----------------------------------------------
 
-// Wavenumber tables of the data grid (FP64, FFTW order) as device pointers.
+// Wavenumber tables of the data grid (FFTW order) as device pointers: FP64, and their FP32
+// roundings for the single-precision kernels (absent where a caller builds a table of its own).
 struct KTab {
-  const double* k[3];
+  const double* k[3] = {nullptr, nullptr, nullptr};
+  const float* k32[3] = {nullptr, nullptr, nullptr};
 };
+
+// Wavenumber of axis d at index i in the arithmetic type CT (FP32 reads the FP32 table when present).
+template <typename CT>
+__device__ __forceinline__ CT ktab_at(const KTab& kt, int d, int i) {
+  if constexpr (sizeof(CT) == 4) {
+    if (kt.k32[d]) return kt.k32[d][i];
+  }
+  return (CT)kt.k[d][i];
+}
 
 // Describes one half-spectrum field to build on the transform grid: Herm(op(F)) with
 //   op(F)(k) = scale * F[src][comp](k) * keep(k) * [shell(k) == band] * (i ks_d(k) if deriv >= 0).

@@ -22,6 +22,7 @@ struct fit_plan {
   int ax_init[3] = {0, 0, 0};
   std::vector<double> ks_host[3];
   double* ks_dev[3] = {nullptr, nullptr, nullptr};
+  float* ks32_dev[3] = {nullptr, nullptr, nullptr};
   fit::KTab kt;
   cudaStream_t stream = nullptr;
   bool own_stream = false;

@@ -192,10 +192,14 @@ static int ct_cols32(int N) {   // CtTile<float2, N>::C
 }
 
 // H (Hermitian part of the masked / embedded velocity), band shell, effective carrier and
-// binning shell for every live half-spectrum mode, compact layout [c][kz'][kx + KX ky'].
-__global__ void k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, const void* F, int f64, int inv,
-                           int two_thirds, const uint16_t* __restrict__ shell, float2* H, float2* Ceff,
-                           uint16_t* seff, uint16_t* sb) {
+// binning shell for every live half-spectrum mode, compact layout [c][kz'][kx + KX ky']. CT is the
+// arithmetic type: FP32 for complex64 input (H and Ceff are stored in FP32), FP64 otherwise.
+template <typename CT>
+__global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, const void* F,
+                                                  int f64, int inv, int two_thirds,
+                                                  const uint16_t* __restrict__ shell, float2* H, float2* Ceff,
+                                                  uint16_t* seff, uint16_t* sb) {
+  typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= P1 * KY) return;
   const long col = i % P1;
@@ -205,23 +209,26 @@ __global__ void k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, 
   map_pair(g, kx, fmod_pos(ky - K, g.M[1]), fmod_pos(kz - K, g.M[2]), &kA, &kB);
   const bool okA = kA.lin >= 0 && (!two_thirds || keep23(g, kA.k));
   const bool okB = kB.lin >= 0 && (!two_thirds || keep23(g, kB.k));
+#pragma unroll
   for (int c = 0; c < 3; ++c) {
-    double2 acc = make_double2(0, 0);
-    if (okA) { const double2 v = ld_c(F, f64, kA.lin + g.Ntot * c); acc.x += v.x; acc.y += v.y; }
-    if (okB) { const double2 v = ld_c(F, f64, kB.lin + g.Ntot * c); acc.x += v.x; acc.y -= v.y; }
-    H[((long)c * KY + kz) * P1 + col] = make_float2((float)(0.5 * acc.x), (float)(0.5 * acc.y));
+    C2 acc = mkc<C2>(0, 0);
+    if (okA) { const C2 v = ld_ct<CT>(F, f64, kA.lin + g.Ntot * c); acc.x += v.x; acc.y += v.y; }
+    if (okB) { const C2 v = ld_ct<CT>(F, f64, kB.lin + g.Ntot * c); acc.x += v.x; acc.y -= v.y; }
+    H[((long)c * KY + kz) * P1 + col] = make_float2((float)((CT)0.5 * acc.x), (float)((CT)0.5 * acc.y));
   }
   sb[(long)kz * P1 + col] = kA.lin >= 0 ? shell[kA.lin] : (kB.lin >= 0 ? shell[kB.lin] : 0);
   const bool A = kA.lin >= 0;
   const bool B = kB.lin >= 0 && kx >= 1 && (g.padded ? true : (2 * kx < g.N[0]));
   uint16_t sh = A ? shell[kA.lin] : (B ? shell[kB.lin] : 0);
   if (two_thirds && (A || B) && !keep23(g, A ? kA.k : kB.k)) sh = 0;
-  double2 CA[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-  double2 CB[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+  C2 CA[3], CB[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) CA[c] = CB[c] = mkc<C2>(0, 0);
   if (sh) {
-    if (A) carrier_at(g, kt, F, f64, g.Ntot, 3, inv, kA.lin, kA.k, CA);
-    if (B) carrier_at(g, kt, F, f64, g.Ntot, 3, inv, kB.lin, kB.k, CB);
+    if (A) carrier_at_t<CT>(g, kt, F, f64, g.Ntot, 3, inv, kA.lin, kA.k, CA);
+    if (B) carrier_at_t<CT>(g, kt, F, f64, g.Ntot, 3, inv, kB.lin, kB.k, CB);
   }
+#pragma unroll
   for (int c = 0; c < 3; ++c)
     Ceff[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
   seff[(long)kz * P1 + col] = sh;
@@ -281,9 +288,12 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   uint16_t* sbp = (uint16_t*)s->fsb.p;
   const long nset = P1 * KY;
   fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
-  k_fz_setup<<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv,
-                                                                    p->dealias == 1, (const uint16_t*)p->shell_full.p,
-                                                                    H, Ce, se, sbp);
+  if (p->io_f64)
+    k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
+        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp);
+  else
+    k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
+        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   // advecting velocity in physical space (once per call)
