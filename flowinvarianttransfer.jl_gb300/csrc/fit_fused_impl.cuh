@@ -622,8 +622,9 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MI
   }
   if (cur) atomicAdd(&bins[cur - 1], sum);
   __syncthreads();
-  double* pb = partial + ((long)b * gridDim.z + blockIdx.z) * a.nsh;
-  for (int t = tid; t < a.nsh; t += NT) pb[t] = bins[t];
+  // partials laid out [mediator][shell][block] so that each shell's reduction reads contiguously
+  double* pb = partial + (long)b * a.nsh * gridDim.z + blockIdx.z;
+  for (int t = tid; t < a.nsh; t += NT) pb[(long)t * gridDim.z] = bins[t];
 }
 
 // Raise the dynamic shared-memory limit and size the carveout for the kernel's occupancy.

@@ -234,13 +234,23 @@ __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, in
   seff[(long)kz * P1 + col] = sh;
 }
 
-__global__ void k_fz_reduce(const double* __restrict__ partial, int npt, FzArgs a, double* Td) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= a.nb * a.nsh) return;
-  const int b = j / a.nsh, n = j % a.nsh;
+// One block per (mediator, shell): the npt block partials of that shell, summed in a fixed order
+// (strided per thread, then a fixed tree), written to T(:, mediator).
+__global__ void __launch_bounds__(256) k_fz_reduce(const double* __restrict__ partial, int npt, FzArgs a,
+                                                   double* Td) {
+  const int b = blockIdx.x / a.nsh, n = blockIdx.x % a.nsh;
+  const double* pp = partial + ((long)b * a.nsh + n) * npt;
   double s = 0.0;
-  for (int t = 0; t < npt; ++t) s += partial[((long)b * npt + t) * a.nsh + n];
-  Td[(long)(a.med[b] - 1) * a.nsh + n] = s;
+  for (int t = threadIdx.x; t < npt; t += blockDim.x) s += pp[t];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ double ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += ws[w];
+    Td[(long)(a.med[b] - 1) * a.nsh + n] = r;
+  }
 }
 
 static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {
@@ -343,8 +353,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
       if (rc == 1) fit_set_error("no fused kernels for size %d", M);
       return rc == 1 ? FIT_ERR_SIZE : rc;
     }
-    k_fz_reduce<<<(unsigned)((a.nb * nsh + 127) / 128), 128, 0, p->stream>>>((const double*)s->fpart.p, (int)npt, a,
-                                                                              Td);
+    k_fz_reduce<<<(unsigned)(a.nb * nsh), 256, 0, p->stream>>>((const double*)s->fpart.p, (int)npt, a, Td);
     FIT_LAUNCH_CHECK();
   }
   return FIT_OK;
