@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--train-steps", type=int, default=1500)
     ap.add_argument("--train-batch", type=int, default=65536)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--mixed", type=int, default=1, help="closure network as a residual over the gradient model")
     return ap.parse_args()
 
 
@@ -482,7 +483,7 @@ def run_closure(args):
         e1.record()
         torch.cuda.synchronize()
         exact_ms = e0.elapsed_time(e1)
-        m = F.SubfilterStressMLP(seed=args.seed)
+        m = F.SubfilterStressMLP(seed=args.seed, mixed=args.mixed)
         t0 = time.perf_counter()
         hist = m.train(d, 0, half, steps=args.train_steps, batch=args.train_batch, lr=args.lr,
                        log_every=max(1, args.train_steps // 5))
@@ -515,7 +516,9 @@ def run_closure(args):
             "vs_baseline": None, "dtype": "bf16 (FP32 accumulation)", "data": "synthetic",
             "config": {"workload": f"{N}^3 D=3 forced SSP-RK3 NS ({args.closure_nsteps} steps, nu={nu}, dt={dt}, "
                                    f"forcing 0<|k|<={kf} at power {power}) from k^4 exp(-2(k/8)^2); Gaussian filter "
-                                   "k_c in {8,16,32}, ell = pi/k_c; MLP 9-64-64-6 trained on z < N/2, scored on z >= N/2",
+                                   "k_c in {8,16,32}, ell = pi/k_c; MLP 9-64-64-6 (homogeneous form" +
+                                   (", residual over the gradient model" if args.mixed else "") +
+                                   ") trained on z < N/2, scored on z >= N/2",
                        "seed": args.seed},
             "evolve": {"ms_per_rk3_step": evolve_ms, "launches_per_step": evolve_launches, "energy": energy},
             "flop_per_point": flop_pt, "results": results}

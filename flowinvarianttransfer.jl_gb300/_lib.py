@@ -18,7 +18,7 @@ EXPORTS = [
     "fit_mlp_train_grad", "fit_mlp_adam", "fit_gradient_model_flux", "fit_field_moments", "fit_field_compare",
     "fit_batch_create", "fit_batch_destroy", "fit_batch_add_flux", "fit_batch_run", "fit_batch_run_eager", "fit_batch_info",
     "fit_autotune_enable", "fit_autotune_clear", "fit_autotune_info", "fit_autotune_entry",
-    "fit_partial_fluxes_batched", "fit_band_to_band",
+    "fit_partial_fluxes_batched", "fit_band_to_band", "fit_stress_residual",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -61,7 +61,8 @@ def _declare(lib):
     lib.fit_forward_spectrum.argtypes = [vp, vp, vp, i32]
     lib.fit_ns_evolve.argtypes = [vp, vp, i32, C.c_double, C.c_double, C.c_double, C.c_double, i32]
     lib.fit_mlp_nparams.argtypes = []
-    lib.fit_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp, i32, vp, vp, vp]
+    lib.fit_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp, i32, C.c_double, vp, vp, vp]
+    lib.fit_stress_residual.argtypes = [vp, vp, i64, i64, C.c_double, vp, vp]
     lib.fit_mlp_train_grad.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, i32, vp, vp, vp]
     lib.fit_gradient_model_flux.argtypes = [vp, i64, i64, C.c_double, vp, vp, vp]
     lib.fit_field_moments.argtypes = [vp, i64, i64, i32, vp, vp]

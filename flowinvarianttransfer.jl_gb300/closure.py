@@ -222,9 +222,12 @@ class SubfilterStressMLP:
 
     ``homogeneous`` (default): the network sees the direction v/|v| of the scaled gradient tensor
     and its output is multiplied by s = |v|^2, so the predicted stress is homogeneous of degree 2
-    in A, as the exact subfilter stress is at leading order in ell."""
+    in A, as the exact subfilter stress is at leading order in ell.
+    ``mixed``: the network learns the residual over the gradient (Clark) model, whose stress
+    ell^2/12 A A^T is added in the forward kernel's epilogue (the filter scale is the training
+    data's)."""
 
-    def __init__(self, seed=0, device=None, params=None, homogeneous=True):
+    def __init__(self, seed=0, device=None, params=None, homogeneous=True, mixed=False):
         torch = _torch()
         self.lib = _lib.load()
         self.nparam = int(self.lib.fit_mlp_nparams())
@@ -242,6 +245,8 @@ class SubfilterStressMLP:
         self.step = 0
         self.device = dev
         self.homogeneous = bool(homogeneous)
+        self.mixed = bool(mixed)
+        self.ell = 0.0
 
     # scales: unit variance of every feature and target over the training points
     def fit_scales(self, X, T, ld, P):
@@ -272,7 +277,8 @@ class SubfilterStressMLP:
         """Adam on random contiguous slabs of ``batch`` points from [p0, p1); cosine learning-rate decay.
         Returns the list of (step, mean scaled loss) at ``log_every``."""
         rng = np.random.default_rng(seed)
-        X, T, ld = data.A, data.tau, data.n
+        self.ell = float(data.ell)
+        X, T, ld = data.A, self.targets(data), data.n
         self.fit_scales(X[:, p0:], T[:, p0:], ld, p1 - p0)
         hist = []
         for s in range(steps):
@@ -288,13 +294,27 @@ class SubfilterStressMLP:
                 hist.append((s, float(self.loss.item()) / (6 * P)))
         return hist
 
+    def targets(self, data: ClosureData):
+        """The training targets: the exact stress, or its residual over the gradient model."""
+        if not self.mixed:
+            return data.tau
+        torch = _torch()
+        R = getattr(data, "residual", None)
+        if R is None or getattr(data, "residual_ell", None) != data.ell:
+            R = torch.empty_like(data.tau)
+            check(self.lib.fit_stress_residual(_vp(data.A), _vp(data.tau), data.n, data.n, data.ell, _vp(R),
+                                               _stream()))
+            data.residual, data.residual_ell = R, data.ell
+        return R
+
     def predict(self, X, ld, P, want_tau=True, want_flux=True):
         """Predicted stress (6, P) and/or flux (P) for points [0, P) of X (stride ld)."""
         torch = _torch()
         Y = torch.empty((6, ld), dtype=torch.float32, device=self.device) if want_tau else None
         Pi = torch.empty(P, dtype=torch.float32, device=self.device) if want_flux else None
         check(self.lib.fit_mlp_forward(_vp(self.params), _vp(X), ld, P, _vp(self.in_scale), _vp(self.t_scale),
-                                       int(self.homogeneous), _vp(Y), _vp(Pi), _stream()))
+                                       int(self.homogeneous), self.ell if self.mixed else 0.0, _vp(Y), _vp(Pi),
+                                       _stream()))
         return (Y[:, :P] if Y is not None else None), Pi
 
     def evaluate(self, data: ClosureData, p0, p1):

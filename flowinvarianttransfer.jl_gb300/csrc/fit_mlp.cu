@@ -167,6 +167,15 @@ FIT_D void mlp_load_x(const float* __restrict__ X, long ld, long P, long p0, con
   xa[3] = pack_bf16(v[1][1][0], v[1][1][1]);
 }
 
+// Gradient-model stress component o (00 11 22 01 02 12) without its ell^2/12 factor: sum_k A_ik A_jk.
+FIT_D float gradient_model_stress(int o, const float* __restrict__ X, long ld, long p) {
+  const int i = o < 3 ? o : (o == 5 ? 1 : 0), j = o < 3 ? o : (o == 3 ? 1 : 2);
+  float t = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) t += X[(long)(3 * i + k) * ld + p] * X[(long)(3 * j + k) * ld + p];
+  return t;
+}
+
 // Pi = -tau_ij S_ij of the predicted stress, S = (A + A^T)/2 (the closure's flux, fused epilogue).
 FIT_D float stress_dot_strain(int o, float tau, const float* __restrict__ X, long ld, long p) {
   const int i = o < 3 ? o : (o == 5 ? 1 : 0), j = o < 3 ? o : (o == 3 ? 1 : 2);
@@ -177,7 +186,7 @@ FIT_D float stress_dot_strain(int o, float tau, const float* __restrict__ X, lon
 __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ Pm, const float* __restrict__ X,
                                                      long ld, long P, const float* __restrict__ in_scale,
                                                      const float* __restrict__ t_scale, float* __restrict__ Y,
-                                                     float* __restrict__ Pi, int homog) {
+                                                     float* __restrict__ Pi, int homog, float clark) {
   __shared__ MlpSmem w;
   __shared__ float sc[9], osc[6];
   mlp_load_weights(&w, Pm, threadIdx.x, blockDim.x);
@@ -201,7 +210,8 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ P
       for (int e = 0; e < 2; ++e) {
         const int o = 2 * t + e;
         if (o < 6 && p < P) {
-          const float tau = y[2 * r + e] * sn[r] * osc[o];
+          float tau = y[2 * r + e] * sn[r] * osc[o];
+          if (clark != 0.f) tau += clark * gradient_model_stress(o, X, ld, p);
           if (Y) Y[(long)o * ld + p] = tau;
           if (Pi) part += stress_dot_strain(o, tau, X, ld, p);
         }
@@ -457,6 +467,15 @@ __global__ void k_gradient_model(const float* __restrict__ X, long ld, long P, f
   if (Pi) Pi[p] = pi;
 }
 
+// out = tau - ell^2/12 A A^T: the targets of the network's residual over the gradient model.
+__global__ void k_stress_residual(const float* __restrict__ X, const float* __restrict__ tau, long ld, long P, float c,
+                                  float* __restrict__ out) {
+  const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (p >= P) return;
+#pragma unroll
+  for (int o = 0; o < 6; ++o) out[(long)o * ld + p] = tau[(long)o * ld + p] - c * gradient_model_stress(o, X, ld, p);
+}
+
 // FP64 block sums of nq quantities per thread, one atomicAdd per block and quantity.
 template <int NQ>
 FIT_D void block_sums_to(double (&q)[NQ], double* out) {
@@ -511,7 +530,8 @@ using namespace fit;
 extern "C" int fit_mlp_nparams(void) { return MLP_NPARAM; }
 
 extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
-                               const float* t_scale, int homogeneous, float* Y, float* Pi, void* stream) {
+                               const float* t_scale, int homogeneous, double clark_ell, float* Y, float* Pi,
+                               void* stream) {
   if (!params || !X || !in_scale || !t_scale || (!Y && !Pi) || P < 0 || ld < P) {
     fit_set_error("bad argument (need params, X, scales, one of Y/Pi, 0 <= P <= ld)");
     return FIT_ERR_ARG;
@@ -521,7 +541,8 @@ extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, 
   const long ntile = (P + 15) / 16;
   long blocks = (ntile + 7) / 8;
   if (blocks > 152 * 8) blocks = 152 * 8;
-  k_mlp_forward<<<(unsigned)blocks, 256, 0, st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi, homogeneous);
+  k_mlp_forward<<<(unsigned)blocks, 256, 0, st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi, homogeneous,
+                                                   (float)(clark_ell * clark_ell / 12.0));
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -602,6 +623,19 @@ extern "C" int fit_field_compare(const float* a, const float* b, int64_t P, doub
   long blocks = (P + 255) / 256;
   if (blocks > 152 * 8) blocks = 152 * 8;
   k_compare<<<(unsigned)blocks, 256, 0, st>>>(a, b, P, out);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+extern "C" int fit_stress_residual(const float* A, const float* tau, int64_t ld, int64_t P, double ell, float* out,
+                                   void* stream) {
+  if (!A || !tau || !out || P < 0 || ld < P || !(ell > 0.0)) {
+    fit_set_error("bad argument (need A, tau, out, 0 <= P <= ld, ell > 0)");
+    return FIT_ERR_ARG;
+  }
+  if (P == 0) return FIT_OK;
+  k_stress_residual<<<(unsigned)((P + 255) / 256), 256, 0, (cudaStream_t)stream>>>(A, tau, ld, P,
+                                                                                  (float)(ell * ell / 12.0), out);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }

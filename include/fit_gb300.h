@@ -217,9 +217,13 @@ int fit_autotune_entry(int64_t i, int64_t* fields, double* ms);
  * pointers are device pointers; stream may be NULL. */
 int fit_mlp_nparams(void);
 /* Y (6 x ld, optional) = predicted stress; Pi (P, optional) = -tau_ij S_ij of the prediction with
- * S = (A + A^T)/2 taken from the unscaled features (the closure's flux, fused). */
+ * S = (A + A^T)/2 taken from the unscaled features (the closure's flux, fused). clark_ell > 0: the
+ * network is a residual over the gradient model and ell^2/12 A A^T is added to its output. */
 int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
-                    const float* t_scale, int homogeneous, float* Y, float* Pi, void* stream);
+                    const float* t_scale, int homogeneous, double clark_ell, float* Y, float* Pi, void* stream);
+/* out (6 x ld) = tau - ell^2/12 A A^T: residual targets of a network trained over the gradient model. */
+int fit_stress_residual(const float* A, const float* tau, int64_t ld, int64_t P, double ell, float* out,
+                        void* stream);
 /* Adds to grad (not cleared) the gradient of loss = sum_p sum_o (s_p y_po - t_scale_o T_op)^2 / Ptot
  * (y: network output, s_p = 1 unless homogeneous) over the P points given (Ptot: points of the
  * whole minibatch, for split calls), and to *loss the sum of squared scaled errors. */

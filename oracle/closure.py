@@ -112,9 +112,10 @@ def _f32(x):
     return np.asarray(x, dtype=np.float32).astype(np.float64)
 
 
-def mlp_forward(params, X, in_scale, t_scale, emulate_bf16=False, homogeneous=False):
+def mlp_forward(params, X, in_scale, t_scale, emulate_bf16=False, homogeneous=False, clark_ell=0.0):
     """X: (9, P) features; returns (Y (6, P) in target units, cache). ``homogeneous``: the network
-    sees v/|v| (v: scaled features) and its output is multiplied by s = |v|^2."""
+    sees v/|v| (v: scaled features) and its output is multiplied by s = |v|^2. ``clark_ell`` > 0:
+    the gradient-model stress at that filter scale is added (the network is a residual)."""
     d = mlp_unpack(params)
     r = bf16 if emulate_bf16 else (lambda v: v)
     W1, W2, W3 = r(d["W1"]), r(d["W2"]), r(d["W3"])
@@ -134,6 +135,8 @@ def mlp_forward(params, X, in_scale, t_scale, emulate_bf16=False, homogeneous=Fa
     h2 = r(np.maximum(z2, 0))
     y = h2 @ W3.T + d["b3"]
     Y = (y[:, :6] * s[:, None] / np.asarray(t_scale, np.float64)).T
+    if clark_ell > 0:
+        Y = Y + clark_stress(np.asarray(X, np.float64), clark_ell)
     return Y, dict(x=x, h1=h1, h2=h2, y=y, W2=W2, W3=W3, s=s)
 
 

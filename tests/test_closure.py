@@ -241,18 +241,19 @@ def _rel(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("homog", [False, True])
-def test_mlp_forward_matches_oracle(homog):
+@pytest.mark.parametrize("homog,mixed", [(False, False), (True, False), (True, True)])
+def test_mlp_forward_matches_oracle(homog, mixed):
     P, ld = 1000, 1037
     p, X, T, isc, tsc = _mlp_case(P, ld)
-    m = F.SubfilterStressMLP(params=p, homogeneous=homog)
+    m = F.SubfilterStressMLP(params=p, homogeneous=homog, mixed=mixed)
+    m.ell = 0.8 if mixed else 0.0
     m.in_scale.copy_(_dev(isc))
     m.t_scale.copy_(_dev(tsc))
     Y, Pi = m.predict(_dev(X), ld, P)
     Y = Y.cpu().numpy()
     Pi = Pi.cpu().numpy()
-    Ye, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, emulate_bf16=True, homogeneous=homog)
-    Y64, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, homogeneous=homog)
+    Ye, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, emulate_bf16=True, homogeneous=homog, clark_ell=m.ell)
+    Y64, _ = OC.mlp_forward(p, X[:, :P], isc, tsc, homogeneous=homog, clark_ell=m.ell)
     assert _rel(Y, Ye) <= 2e-3           # same BF16 rounding points, FP32 vs FP64 accumulation
     assert _rel(Y, Y64) <= 3e-2          # BF16 quantisation of weights, features and activations
     assert _rel(Pi, OC.flux_from_stress(Y.astype(np.float64), X[:, :P].astype(np.float64))) <= 1e-5
@@ -319,6 +320,26 @@ def test_gradient_model_and_compare():
 
 
 @pytest.mark.gpu
+def test_stress_residual_matches_oracle():
+    import ctypes as C
+    import torch
+    rng = np.random.default_rng(12)
+    P, ld = 777, 800
+    A = np.zeros((9, ld), np.float32)
+    tau = np.zeros((6, ld), np.float32)
+    A[:, :P] = rng.standard_normal((9, P))
+    tau[:, :P] = rng.standard_normal((6, P))
+    Ad, td = _dev(A), _dev(tau)
+    out = torch.zeros((6, ld), dtype=torch.float32, device="cuda")
+    lib = F._lib.load()
+    F._lib.check(lib.fit_stress_residual(C.c_void_p(Ad.data_ptr()), C.c_void_p(td.data_ptr()), ld, P, 0.6,
+                                         C.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    ref = tau[:, :P].astype(np.float64) - OC.clark_stress(A[:, :P].astype(np.float64), 0.6)
+    assert _rel(out.cpu().numpy()[:, :P], ref) <= 1e-6
+
+
+@pytest.mark.gpu
 def test_closure_data_matches_oracle():
     import torch
     ns = (32, 32, 32)
@@ -353,11 +374,14 @@ def test_learned_closure_gain():
     d = F.closure_data(u_dev, ks, np.pi / 8)
     n = d.n
     res = {}
-    for homog in (False, True):
-        m = F.SubfilterStressMLP(seed=0, homogeneous=homog)
+    for homog, mixed in ((False, False), (True, False), (True, True)):
+        m = F.SubfilterStressMLP(seed=0, homogeneous=homog, mixed=mixed)
         hist = m.train(d, 0, n // 2, steps=800, batch=16384, lr=3e-3, log_every=100)
-        res[homog] = ev = m.evaluate(d, n // 2, n)
-        print(homog, hist, ev)
+        res[(homog, mixed)] = ev = m.evaluate(d, n // 2, n)
+        print(homog, mixed, hist, ev)
         assert hist[-1][1] < hist[0][1]
         assert ev["rel_l2_mlp"] < 0.6 * ev["rel_l2_no_closure"]
         assert ev["corr_mlp"] > 0.75
+    # the residual network keeps the gradient model's accuracy and adds to it
+    ev = res[(True, True)]
+    assert ev["rel_l2_mlp"] <= ev["rel_l2_gradient_model"] * 1.02
