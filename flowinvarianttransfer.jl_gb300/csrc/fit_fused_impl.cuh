@@ -663,11 +663,22 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   const unsigned pt = (unsigned)((a.P1 + C - 1) / C);
   const unsigned nkt = (unsigned)((a.KX + C - 1) / C);
   const double cpx = 8.0;
-  fit_prof_begin(PK_S2S_ZINV, cpx * a.nb * (3.0 * a.KY * a.P1 + 6.0 * N * a.P1) + 2.0 * a.nb * a.KY * a.P1, st);
+  // algorithmic bytes of the pruned passes (lower bounds of what they move): mediator b has
+  // Pm = (ex+1)(2ey+1) live pencils; zinv reads the band map on 2ez+1 z frequencies of each (the
+  // velocity itself only on the shell's own modes, not counted) and writes 6 N-long outputs; yinv
+  // reads the 6 zinv outputs of those pencils once and writes 9 outputs of N x N x (ex+1) values
+  double zin_b = 0.0, yin_b = 0.0;
+  for (int b = 0; b < a.nb; ++b) {
+    const double ex = a.ext[b][0], ey = a.ext[b][1], ez = a.ext[b][2];
+    const double Pm = (ex + 1.0) * (2.0 * ey + 1.0);
+    zin_b += cpx * 6.0 * N * Pm + 2.0 * (2.0 * ez + 1.0) * Pm;
+    yin_b += cpx * (6.0 * N * Pm + 9.0 * (double)N * N * (ex + 1.0));
+  }
+  fit_prof_begin(PK_S2S_ZINV, zin_b, st);
   k_fz_zinv<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, sb, kd, bufA, tw);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
-  fit_prof_begin(PK_S2S_YINV, cpx * a.nb * (6.0 * N * a.P1 + 9.0 * (double)N * N * a.KX), st);
+  fit_prof_begin(PK_S2S_YINV, yin_b, st);
   k_fz_yinv<N><<<dim3(a.nb, 9, nkt * N), TT::NTHR, sm, st>>>(a, bufA, kd, bufB, tw);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
