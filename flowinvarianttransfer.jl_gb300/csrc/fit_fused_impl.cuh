@@ -43,6 +43,7 @@ struct FzArgs {
   short ext[16][3];   // per mediator: largest |signed frequency| of its shell's modes along x, y, z
   float sp;     // 1 / Mtot (physical-space normalisation of the inverse transforms)
   float so;     // output normalisation of the forward transform (1/Ntot, or Mtot/Ntot^2 padded)
+  int xpair;    // x pass: complex column c carries lines (2c, 2c+1) (0) or (c, c+C) (1) of its tile
 };
 
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
@@ -416,6 +417,11 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
   const int b = blockIdx.x;
   const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
   const long Mtot = (long)N * N * N;
+  // the two lines of complex column c: gradient rows ra, rb of the (line-ordered) staging tile;
+  // velocity line r lands in row urow(r), so that column c reads velocity rows c and c + C
+  // (4-bank row offsets with rows of N + 4 floats: conflict-free for a warp's 8 columns)
+  const int xp = a.xpair;
+  auto urow = [&](int r) -> int { return xp ? r : (r & 1) * C + (r >> 1); };
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -429,7 +435,7 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
     mbar_expect_tx(&bar[0], gbytes);
     bulk_g2s(stg, G + (gb + l0) * a.KX, gbytes, &bar[0]);
     mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
-    for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + r * TT::UP, U + (l0 + r) * N, (uint32_t)(N * 4), &bar[2]);
+    for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + urow(r) * TT::UP, U + (l0 + r) * N, (uint32_t)(N * 4), &bar[2]);
   }
   // after a timed-out wait: give the copies this block still has in flight a bounded chance to
   // land before the block exits (gradient tiles t and t+1, velocity tile t)
@@ -470,8 +476,9 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           const int kk = cj ? N - k : k;
           float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
           if (kk <= ex) {
-            A = sg[(2 * col) * a.KX + kk];
-            B = sg[(2 * col + 1) * a.KX + kk];
+            const int ra = xp ? col : 2 * col, rb = xp ? col + C : 2 * col + 1;
+            A = sg[ra * a.KX + kk];
+            B = sg[rb * a.KX + kk];
             if (j == 0) {
               const float kx = kd[a.K + kk];
               A = fz_muli(A, kx);
@@ -487,8 +494,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           return !__syncthreads_or(!oku);
         },
         [&](int i, int q, int x, int col, float2 zv) {
-          acc[i][q].x += us[(2 * col) * TT::UP + x] * (zv.x * sp);
-          acc[i][q].y += us[(2 * col + 1) * TT::UP + x] * (zv.y * sp);
+          acc[i][q].x += us[col * TT::UP + x] * (zv.x * sp);
+          acc[i][q].y += us[(col + C) * TT::UP + x] * (zv.y * sp);
         });
     if (!ok) {
       if (tid == 0) atomicExch(err, 1);
@@ -501,7 +508,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
       const float* src = U + (long)j1 * Mtot + l0 * N;
-      for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + r * TT::UP, src + (long)r * N, (uint32_t)(N * 4), &bar[2]);
+      for (int r = 0; r < 2 * C; ++r)
+        bulk_g2s(us + urow(r) * TT::UP, src + (long)r * N, (uint32_t)(N * 4), &bar[2]);
     }
     if (j == 2) {
       ct_fft_mapped<float2, false, N, C, NT, EPT>(
@@ -510,9 +518,11 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
       __syncthreads();
       const long obase = ((long)b * 3 + c) * a.L;
       const float hs = 0.5f * a.so;
+      // column fastest: a warp reads 4 whole swizzled rows of s (no bank conflicts) and writes
+      // 32-byte runs of 8 lines
       for (int i = tid; i < C * a.KX; i += NT) {
-        const int col = i / a.KX, k = i % a.KX;
-        const long la = l0 + 2 * col, lb = la + 1;
+        const int col = i % C, k = i / C;
+        const long la = l0 + (xp ? col : 2 * col), lb = la + (xp ? C : 1);
         const float2 zk = s[swz(k, col, C)];
         const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
         out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
@@ -646,6 +656,34 @@ static int ct_prep_fused(K kern, size_t smem, int nthr) {
   return FIT_OK;
 }
 
+// Line pairing of the x pass with the fewer shared-memory bank conflicts on the gradient tile:
+// a half-warp reads 8-byte elements at rows row(c) of stride KX for its columns c = lane % C and
+// consecutive positions lane / C; the busiest bank's distinct-word count is compared.
+static int fz_xpair(int KX, int C) {
+  int best = 0, best_hits = 1 << 30;
+  for (int mode = 0; mode < 2; ++mode) {
+    int words[16], hits = 0;
+    for (int lane = 0; lane < 16; ++lane) {
+      const int c = lane % C, j = lane / C;
+      words[lane] = 2 * ((mode ? c : 2 * c) * KX + j);
+    }
+    for (int bank = 0; bank < 32; ++bank) {
+      int distinct[32], nd = 0;
+      for (int lane = 0; lane < 16; ++lane)
+        for (int h = 0; h < 2; ++h) {
+          const int w = words[lane] + h;
+          if (w % 32 != bank) continue;
+          bool seen = false;
+          for (int t = 0; t < nd; ++t) seen = seen || distinct[t] == w;
+          if (!seen) distinct[nd++] = w;
+        }
+      if (nd > hits) hits = nd;
+    }
+    if (hits < best_hits) best_hits = hits, best = mode;
+  }
+  return best;
+}
+
 // ---- host launcher for one batch (instantiated per transform length) -------------------------
 template <int N>
 int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff, const uint16_t* sb,
@@ -695,8 +733,10 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
     if constexpr (XR::OK) {
       if (reg) {
         FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
-        k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(a, bufB, U, kd, bufA,
-                                                                                             tw, err);
+        FzArgs ax = a;
+        ax.xpair = fz_xpair(a.KX, XR::C);
+        k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, bufB, U, kd, bufA,
+                                                                                              tw, err);
       }
     }
     if (reg) {

@@ -263,8 +263,12 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   const long npt = (P1 + C - 1) / C;
   const double perA = (double)(6.0 * M * P1 > 3.0 * L * KX ? 6.0 * M * P1 : 3.0 * L * KX);
   const double perB = (double)(9.0 * L * KX > 3.0 * M * P1 ? 9.0 * L * KX : 3.0 * M * P1);
+  std::vector<int> meds;   // mediators with at least one mode
+  for (int m = 1; m <= nsh; ++m)
+    if (s->occ[m - 1] > 0) meds.push_back(m);
   int B = (int)(40e9 / (8.0 * (perA + perB)));
   if (B > 16) B = 16;
+  if (B > (int)meds.size()) B = (int)meds.size();   // no scratch for batch slots that never fill
   if (B < 1) B = 1;
   FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 3 * KY * P1));
   FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * KY * P1));
@@ -321,9 +325,6 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   FIT_TRY(gather_half<float>(g, p->kt, ga, (float2*)p->hs.p, p->stream));
   FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)(1.0 / (double)g.Mtot),
                             p->stream));
-  std::vector<int> meds;
-  for (int m = 1; m <= nsh; ++m)
-    if (s->occ[m - 1] > 0) meds.push_back(m);
   FzArgs a;
   memset(&a, 0, sizeof(a));
   a.K = K;
