@@ -200,6 +200,49 @@ static int stage_in(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int
   }
   FIT_TRY(ensure(p, b, bytes));
   FIT_CUDA_CHECK(cudaMemcpyAsync(b->p, src, bytes, cudaMemcpyHostToDevice, p->stream));
+  p->h2d_total += bytes;
+  *out = b->p;
+  return FIT_OK;
+}
+
+// Host inputs of a path that reads only the 2/3-kept modes: copy just the box of modes every axis
+// keeps (indices [0, K] and [N - K, N) per axis): per component, 8 pitched 3D copies (one per
+// octant of the box). Modes outside the box are left unwritten in the staging buffer and are
+// never read.
+static int stage_in_kept_box(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int ncomp, const void** out) {
+  if (src == nullptr) {
+    *out = nullptr;
+    return FIT_OK;
+  }
+  FIT_TRY(ensure(p, b, bytes));
+  const GridDesc& g = p->g;
+  const size_t eb = cbytes(p), row = eb * g.N[0], plane = row * g.N[1];
+  int lo[3][2], n[3][2];
+  for (int d = 0; d < 3; ++d) {
+    const int K = g.N[d] / 3 - 1;   // kept iff min(k, N - k) < N / 3
+    lo[d][0] = 0;
+    n[d][0] = K + 1;
+    lo[d][1] = g.N[d] - K;
+    n[d][1] = K;
+  }
+  for (int c = 0; c < ncomp; ++c) {
+    char* dst = (char*)b->p + (size_t)c * plane * g.N[2];
+    const char* hs = (const char*)src + (size_t)c * plane * g.N[2];
+    for (int o = 0; o < 8; ++o) {
+      const int rx = o & 1, ry = (o >> 1) & 1, rz = o >> 2;
+      if (n[0][rx] <= 0 || n[1][ry] <= 0 || n[2][rz] <= 0) continue;
+      cudaMemcpy3DParms cp;
+      memset(&cp, 0, sizeof(cp));
+      cp.srcPtr = make_cudaPitchedPtr((void*)hs, row, row, g.N[1]);
+      cp.dstPtr = make_cudaPitchedPtr(dst, row, row, g.N[1]);
+      cp.srcPos = make_cudaPos((size_t)lo[0][rx] * eb, lo[1][ry], lo[2][rz]);
+      cp.dstPos = cp.srcPos;
+      cp.extent = make_cudaExtent((size_t)n[0][rx] * eb, n[1][ry], n[2][rz]);
+      cp.kind = cudaMemcpyHostToDevice;
+      FIT_CUDA_CHECK(cudaMemcpy3DAsync(&cp, p->stream));
+      p->h2d_total += (size_t)n[0][rx] * eb * n[1][ry] * n[2][rz];
+    }
+  }
   *out = b->p;
   return FIT_OK;
 }
@@ -415,8 +458,9 @@ int fit_plan_set_stream(fit_plan* p, void* stream) {
 
 int fit_plan_info(const fit_plan* p, int64_t* info, int n) {
   API_CHECK(p != nullptr && info != nullptr, FIT_ERR_ARG, "NULL argument");
-  const int64_t v[8] = {p->nd, p->g.N[0], p->g.N[1], p->g.N[2], p->g.M[0], p->g.M[1], p->g.M[2], (int64_t)p->bytes};
-  for (int i = 0; i < n && i < 8; ++i) info[i] = v[i];
+  const int64_t v[9] = {p->nd,      p->g.N[0], p->g.N[1], p->g.N[2], p->g.M[0], p->g.M[1], p->g.M[2], (int64_t)p->bytes,
+                        (int64_t)p->h2d_total};
+  for (int i = 0; i < n && i < 9; ++i) info[i] = v[i];
   return FIT_OK;
 }
 
@@ -532,8 +576,13 @@ int fit_shell_to_shell(fit_plan* p, const void* u_hat, const void* adv_hat, cons
   API_CHECK(mode == FIT_S2S_PLAIN || mode == FIT_S2S_BATCHED, FIT_ERR_ARG, "unknown shell-to-shell mode %d", mode);
   const size_t fb = cbytes(p) * p->g.Ntot * p->M, ab = cbytes(p) * p->g.Ntot * p->Dadv;
   const void *ud, *ad;
-  FIT_TRY(stage_in(p, &p->in_u, u_hat, fb, ptr_kind, &ud));
-  FIT_TRY(stage_in(p, &p->in_a, adv_hat, ab, ptr_kind, &ad));
+  if (mode == FIT_S2S_BATCHED && ptr_kind != FIT_PTR_DEVICE && s2s_reads_kept_box(p)) {
+    FIT_TRY(stage_in_kept_box(p, &p->in_u, u_hat, fb, p->M, &ud));
+    FIT_TRY(stage_in_kept_box(p, &p->in_a, adv_hat, ab, p->Dadv, &ad));
+  } else {
+    FIT_TRY(stage_in(p, &p->in_u, u_hat, fb, ptr_kind, &ud));
+    FIT_TRY(stage_in(p, &p->in_a, adv_hat, ab, ptr_kind, &ad));
+  }
   if (!ad) {
     API_CHECK(p->M >= p->nd, FIT_ERR_ARG, "self-advection needs >= nd components (pass advecting_hat)");
     ad = ud;

@@ -532,7 +532,9 @@ struct CtMap {
 // store, so only the inner stage exchanges touch shared memory; otherwise the map is staged through
 // shared memory around the full stage sequence. store may write the element it receives back into s
 // (each thread only rewrites rows it just read). Callers synchronise before reusing s.
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, typename LD, typename ST>
+// LOAD_S: load() reads the tile in s itself; the first stage then waits for every thread's loads
+// before it overwrites s.
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, bool LOAD_S = false, typename LD, typename ST>
 __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD load, ST store) {
   typedef CtMap<N> MP;
   constexpr int RL = MP::RL, NRL = MP::NRL;
@@ -548,8 +550,22 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
 #pragma unroll
         for (int q = 0; q < RL; ++q) v[i][q] = load(i, q, j + q * NRL, c);
         dftr<V, RL, INV>(v[i]);
+        if constexpr (!LOAD_S) {
 #pragma unroll
-        for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+          for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+        }
+      }
+    }
+    if constexpr (LOAD_S) {
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < MB; ++i) {
+        const int b = tid + i * NTHR;
+        if (NB % NTHR == 0 || b < NB) {
+          const int c = b % C, j = b / C;
+#pragma unroll
+          for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+        }
       }
     }
     __syncthreads();

@@ -5,13 +5,13 @@ namespace fit {
 
 // Returns 1 when N is not built in this translation unit.
 int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
-                    const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB,
+                    const float* kd, const float* U, float2* bufA, float2* bufB,
                     double* partial, const float2* tw, int* err, cudaStream_t st) {
   switch (N) {
-    case 64: return fz_batch<64>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
-    case 128: return fz_batch<128>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
-    case 256: return fz_batch<256>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
-    case 512: return fz_batch<512>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
+    case 64: return fz_batch<64>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
+    case 128: return fz_batch<128>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
+    case 256: return fz_batch<256>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
+    case 512: return fz_batch<512>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
     default: return 1;
   }
 }

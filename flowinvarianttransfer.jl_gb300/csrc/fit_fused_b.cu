@@ -5,13 +5,13 @@ namespace fit {
 
 // Returns 1 when N is not built in this translation unit.
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
-                    const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB,
+                    const float* kd, const float* U, float2* bufA, float2* bufB,
                     double* partial, const float2* tw, int* err, cudaStream_t st) {
   switch (N) {
-    case 96: return fz_batch<96>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
-    case 192: return fz_batch<192>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
-    case 384: return fz_batch<384>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
-    case 768: return fz_batch<768>(a, H, Ceff, seff, sb, kd, U, bufA, bufB, partial, tw, err, st);
+    case 96: return fz_batch<96>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
+    case 192: return fz_batch<192>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
+    case 384: return fz_batch<384>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
+    case 768: return fz_batch<768>(a, H, Ceff, seff, kd, U, bufA, bufB, partial, tw, err, st);
     default: return 1;
   }
 }

@@ -18,6 +18,7 @@
 //
 // Layouts (complex64 unless noted): live pencils col = kx + KX*ky' (P1 = KX*KY of them);
 //   H, Ceff   [c][kz'][col]           seff, sb (uint16) [kz'][col]
+//   zoff/zent: the modes with sb == m of each C-pencil tile, listed per (m, tile)
 //   zinv out  [b][c][v][z][col]        yinv out [b][c][j][z][y][kx]
 //   xmix out  [b][c][line = y + N z][kx]   yfwd out [b][c][z][ky'][kx]
 #pragma once
@@ -44,28 +45,36 @@ struct FzArgs {
   float sp;     // 1 / Mtot (physical-space normalisation of the inverse transforms)
   float so;     // output normalisation of the forward transform (1/Ntot, or Mtot/Ntot^2 padded)
   int xpair;    // x pass: complex column c carries lines (2c, 2c+1) (0) or (c, c+C) (1) of its tile
+  // z pass inputs as lists: the modes of band shell m in pencil tile t (C consecutive pencils) are
+  // zent[zoff[(m-1)*ntile + t] .. zoff[(m-1)*ntile + t + 1]), each (kz' << 6) | (pencil - t*C)
+  const unsigned* zoff;
+  const uint16_t* zent;
+  int ntile;
 };
 
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
 FIT_D float2 fz_muli(float2 h, float k) { return make_float2(-h.y * k, h.x * k); }   // i*k*h
 
 // ---- zinv --------------------------------------------------------------------------------------
+// One block per (mediator, component and derivative, pencil tile): the tile's modes of the
+// mediator's shell are scattered from their list into a zeroed tile, then transformed along z.
 template <int N>
 __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_zinv(FzArgs a, const float2* __restrict__ H,
-                                                                    const uint16_t* __restrict__ sb,
                                                                     const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
   typedef CtTile<float2, N> TT;
-  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
+  static_assert(C <= 64 && NT * EPT == E, "zinv: tile column must fit the list entry");
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
   float2* tw = s + E;
   const int tid = threadIdx.x;
-  const long c0 = (long)blockIdx.z * C;
+  const int tile = blockIdx.z;
+  const long c0 = (long)tile * C;
   const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
   const int m = a.med[b];
-  const int ex = a.ext[b][0], ey = a.ext[b][1], ez = a.ext[b][2];
+  const int ex = a.ext[b][0], ey = a.ext[b][1];
   // pencils (kx, ky) outside the mediator's extent hold no mode of its shell: skip the tile (its
   // outputs are never read: yinv and xmix mask with the same extents)
   bool live = false;
@@ -76,27 +85,35 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MI
     live = kx <= ex && ky >= -ey && ky <= ey;
   }
   if (!live) return;
+  const long tl = (long)(m - 1) * a.ntile + tile;
+  const unsigned e0 = a.zoff[tl], e1 = a.zoff[tl + 1];
+  float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1;
+  if (e0 == e1) {   // no mode of the shell in these pencils: the transform is zero
+    for (int i = tid; i < E; i += NT) {
+      const int cc = i % C, e = i / C;
+      if (c0 + cc < a.P1) ob[(long)e * a.P1 + c0 + cc] = make_float2(0.f, 0.f);
+    }
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < EPT; ++r) s[tid + r * NT] = make_float2(0.f, 0.f);
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
-  const long ob = (((long)b * 3 + c) * 2 + v) * N;
-  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
-      s, tw, tid,
-      [&](int, int, int e, int cc) -> float2 {
-        const long col = c0 + cc;
-        const int f = fz_freq(e, N);
-        float2 val = make_float2(0.f, 0.f);
-        if (col < a.P1 && f >= -ez && f <= ez) {
-          const int kz = f + a.K;
-          if (sb[(long)kz * a.P1 + col] == m) {
-            val = H[((long)c * a.KY + kz) * a.P1 + col];
-            if (v) val = fz_muli(val, kd[kz]);
-          }
-        }
-        return val;
-      },
+  const float2* Hc = H + (long)c * a.KY * a.P1 + c0;
+  for (unsigned t = e0 + tid; t < e1; t += NT) {
+    const unsigned en = a.zent[t];
+    const int kz = (int)(en >> 6), cc = (int)(en & 63u);
+    float2 val = Hc[(long)kz * a.P1 + cc];
+    if (v) val = fz_muli(val, kd[kz]);
+    const int f = kz - a.K;
+    s[swz(f < 0 ? f + N : f, cc, C)] = val;
+  }
+  __syncthreads();
+  ct_fft_mapped<float2, true, N, C, NT, EPT, true>(
+      s, tw, tid, [&](int, int, int e, int cc) -> float2 { return s[swz(e, cc, C)]; },
       [&](int, int, int e, int cc, float2 val) {
         const long col = c0 + cc;
-        if (col < a.P1) out[(ob + e) * a.P1 + col] = val;
+        if (col < a.P1) ob[(long)e * a.P1 + col] = val;
       });
 }
 
@@ -686,7 +703,7 @@ static int fz_xpair(int KX, int C) {
 
 // ---- host launcher for one batch (instantiated per transform length) -------------------------
 template <int N>
-int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff, const uint16_t* sb,
+int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
              const float* kd, const float* U, float2* bufA, float2* bufB, double* partial, const float2* tw,
              int* err, cudaStream_t st) {
   typedef CtTile<float2, N> TT;
@@ -713,7 +730,7 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
     yin_b += cpx * (6.0 * N * Pm + 9.0 * (double)N * N * (ex + 1.0));
   }
   fit_prof_begin(PK_S2S_ZINV, zin_b, st);
-  k_fz_zinv<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, sb, kd, bufA, tw);
+  k_fz_zinv<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, kd, bufA, tw);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_YINV, yin_b, st);

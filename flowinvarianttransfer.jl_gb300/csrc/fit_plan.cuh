@@ -28,6 +28,7 @@ struct fit_plan {
   bool own_stream = false;
   size_t bytes = 0;
   long buf_gen = 0;   // bumped on every (re)allocation: captured graphs key on it
+  size_t h2d_total = 0;   // bytes of host inputs copied to the device by this plan's calls
 
   // staging copies of host inputs (user layout, io precision)
   fit_dbuf in_u, in_a, in_c, out_c, out_c2;
@@ -64,6 +65,8 @@ template <typename T>
 int bin_into(fit_plan* p, const void* nh, long bstride, int nb, const void* ceff, double* out);
 int s2s_batched(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, double* Tdev);
 int s2s_check(fit_plan* p);
+// 1 when the batched shell-to-shell path reads the inputs only on the 2/3-kept box of modes
+int s2s_reads_kept_box(const fit_plan* p);
 void s2s_free(fit_plan* p);
 void partial_free(fit_plan* p);
 int triad_m2m(fit_plan* p, const void* u_dev, const void* a_dev, int invariant, int fp64, double* S, double* net);

@@ -15,10 +15,10 @@
 namespace fit {
 
 int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
-                  const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
+                  const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
                   const float2* tw, int* err, cudaStream_t st);
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
-                  const uint16_t* sb, const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
+                  const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
                   const float2* tw, int* err, cudaStream_t st);
 
 struct S2SState {
@@ -38,13 +38,21 @@ struct S2SState {
   // fused-path buffers
   fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr;
   int fkd_n = -1;
+  // per (band shell, pencil tile) lists of the shell's live modes (zinv inputs), rebuilt when the
+  // shell table changes
+  fit_dbuf zoff, zent, zfill;
+  std::vector<double> zl_edges;
+  unsigned zl_dims = 0;
+  int zl_f32 = -1;
+  int zl_nsh = -1;
 };
 
 void s2s_free(fit_plan* p) {
   S2SState* s = (S2SState*)p->s2s;
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
-  fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse, &s->fsb, &s->fkd, &s->fA, &s->fB, &s->fpart, &s->ferr};
+  fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse,  &s->fsb,  &s->fkd,  &s->fA,
+                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill};
   for (fit_dbuf* b : bufs)
     if (b->p) cudaFree(b->p);
   delete s;
@@ -185,6 +193,10 @@ static bool fused_ok(const fit_plan* p) {
   return p->ks_host[0] == p->ks_host[1] && p->ks_host[0] == p->ks_host[2];
 }
 
+// The fused path with the 2/3 rule reads u and the advecting velocity only where every axis keeps
+// the mode (the set-up and gather kernels skip the masked modes' loads).
+int s2s_reads_kept_box(const fit_plan* p) { return fused_ok(p) && p->dealias == 1 ? 1 : 0; }
+
 static int ct_cols32(int N) {   // CtTile<float2, N>::C
   int w = 1;
   while (w * 2 <= 4096 / N) w *= 2;
@@ -232,6 +244,54 @@ __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, in
   for (int c = 0; c < 3; ++c)
     Ceff[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
   seff[(long)kz * P1 + col] = sh;
+}
+
+// Mode lists of the z pass: count the live modes of every (band shell, pencil tile), scan the
+// counts into offsets, then place each mode's entry (kz' << 6 | pencil within tile). Entries of one
+// list land in any order: the z pass scatters them to distinct elements.
+__global__ void k_zl_count(const uint16_t* __restrict__ sb, long nmodes, long P1, int C, int ntile,
+                           unsigned* __restrict__ cnt) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= nmodes) return;
+  const int sh = sb[i];
+  if (sh) atomicAdd(&cnt[(long)(sh - 1) * ntile + (i % P1) / C], 1u);
+}
+
+// Exclusive scan of n counts into off[0..n] (one block: per-thread chunk sums, a block scan of
+// those, then each chunk written in order).
+__global__ void __launch_bounds__(1024) k_zl_scan(const unsigned* __restrict__ cnt, long n, unsigned* __restrict__ off) {
+  __shared__ unsigned part[1024];
+  const int t = threadIdx.x;
+  const long per = (n + 1023) / 1024, lo = t * per, hi = lo + per < n ? lo + per : n;
+  unsigned sum = 0;
+  for (long i = lo; i < hi; ++i) sum += cnt[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {   // inclusive Hillis-Steele scan
+    const unsigned v = t >= o ? part[t - o] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  unsigned run = part[t] - sum;
+  for (long i = lo; i < hi; ++i) {
+    off[i] = run;
+    run += cnt[i];
+  }
+  if (t == 1023) off[n] = part[1023];
+}
+
+__global__ void k_zl_fill(const uint16_t* __restrict__ sb, long nmodes, long P1, int C, int ntile,
+                          const unsigned* __restrict__ off, unsigned* __restrict__ fill, uint16_t* __restrict__ ent) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= nmodes) return;
+  const int sh = sb[i];
+  if (!sh) return;
+  const long col = i % P1;
+  const int kz = (int)(i / P1);
+  const long t = (long)(sh - 1) * ntile + col / C;
+  const unsigned pos = off[t] + atomicAdd(&fill[t], 1u);
+  ent[pos] = (uint16_t)((kz << 6) | (int)(col % C));
 }
 
 // One block per (mediator, shell): the npt block partials of that shell, summed in a fixed order
@@ -310,6 +370,28 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
         g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
+  const int ntile = (int)npt;
+  if (s->zl_edges != p->cached_edges || s->zl_dims != p->cached_dims || s->zl_f32 != p->cached_f32 ||
+      s->zl_nsh != nsh) {   // shell table changed: rebuild the z-pass mode lists (an eager call)
+    const long nmodes = nset, nl = (long)nsh * ntile;
+    FIT_TRY(ensure(p, &s->zoff, sizeof(unsigned) * (size_t)(nl + 1)));
+    FIT_TRY(ensure(p, &s->zfill, sizeof(unsigned) * (size_t)nl));
+    FIT_TRY(ensure(p, &s->zent, sizeof(uint16_t) * (size_t)nmodes));
+    FIT_CUDA_CHECK(cudaMemsetAsync(s->zfill.p, 0, sizeof(unsigned) * (size_t)nl, p->stream));
+    const unsigned gb = (unsigned)((nmodes + 255) / 256);
+    k_zl_count<<<gb, 256, 0, p->stream>>>(sbp, nmodes, P1, C, ntile, (unsigned*)s->zfill.p);
+    FIT_LAUNCH_CHECK();
+    k_zl_scan<<<1, 1024, 0, p->stream>>>((const unsigned*)s->zfill.p, nl, (unsigned*)s->zoff.p);
+    FIT_LAUNCH_CHECK();
+    FIT_CUDA_CHECK(cudaMemsetAsync(s->zfill.p, 0, sizeof(unsigned) * (size_t)nl, p->stream));
+    k_zl_fill<<<gb, 256, 0, p->stream>>>(sbp, nmodes, P1, C, ntile, (const unsigned*)s->zoff.p, (unsigned*)s->zfill.p,
+                                         (uint16_t*)s->zent.p);
+    FIT_LAUNCH_CHECK();
+    s->zl_edges = p->cached_edges;
+    s->zl_dims = p->cached_dims;
+    s->zl_f32 = p->cached_f32;
+    s->zl_nsh = nsh;
+  }
   // advecting velocity in physical space (once per call)
   GatherArgs ga;
   memset(&ga, 0, sizeof(ga));
@@ -335,6 +417,9 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   a.nsh = nsh;
   a.sp = (float)(1.0 / (double)g.Mtot);
   a.so = (float)(g.padded ? (double)g.Mtot / ((double)g.Ntot * (double)g.Ntot) : 1.0 / (double)g.Ntot);
+  a.zoff = (const unsigned*)s->zoff.p;
+  a.zent = (const uint16_t*)s->zent.p;
+  a.ntile = ntile;
   const float2* tw = p->ax[0].tw32;
   for (size_t b0 = 0; b0 < meds.size(); b0 += B) {
     a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
@@ -345,10 +430,10 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
         a.ext[b][d] = (short)(e < K ? e : K);
       }
     }
-    int rc = fz_dispatch_a(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
+    int rc = fz_dispatch_a(M, a, H, Ce, se, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
                            (float2*)s->fB.p, (double*)s->fpart.p, tw, (int*)s->ferr.p, p->stream);
     if (rc == 1)
-      rc = fz_dispatch_b(M, a, H, Ce, se, sbp, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
+      rc = fz_dispatch_b(M, a, H, Ce, se, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
                          (float2*)s->fB.p, (double*)s->fpart.p, tw, (int*)s->ferr.p, p->stream);
     if (rc != FIT_OK) {
       if (rc == 1) fit_set_error("no fused kernels for size %d", M);

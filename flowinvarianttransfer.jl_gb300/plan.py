@@ -65,8 +65,8 @@ class Plan:
         return None if a is None else C.c_void_p(a.ctypes.data)
 
     def info(self):
-        out = (C.c_int64 * 8)()
-        check(self.lib.fit_plan_info(self.h, out, 8))
+        out = (C.c_int64 * 9)()
+        check(self.lib.fit_plan_info(self.h, out, 9))
         return list(out)
 
     def set_stream(self, stream_ptr: int):

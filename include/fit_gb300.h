@@ -67,7 +67,8 @@ int fit_plan_destroy(fit_plan* plan);
 const char* fit_last_error(void);
 /* Use an existing cudaStream_t (passed as void*) instead of the plan's own stream. */
 int fit_plan_set_stream(fit_plan* plan, void* stream);
-/* info[0..7] = nd, N0, N1, N2, M0, M1, M2 (transform grid), bytes of device memory held. */
+/* info[0..8] = nd, N0, N1, N2, M0, M1, M2 (transform grid), bytes of device memory held, bytes of
+ * host inputs copied to the device by the plan's calls so far. */
 int fit_plan_info(const fit_plan* plan, int64_t* info, int n);
 /* Number of library kernels launched since load (graph replays count their kernels). */
 long long fit_launch_count(void);

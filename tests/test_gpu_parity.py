@@ -243,3 +243,23 @@ def test_fused_shell_to_shell_64(deal, inv, herm, xpass, monkeypatch):
     _, _, T, net, _ = O.shell_to_shell(u, ks, ("linear", 4.0), deal, inv)
     assert rel(r.transfer_matrix, T) < 1e-5
     assert rel(r.net_transfer, net) < 1e-4
+
+
+def test_fused_host_input_reads_only_kept_modes():
+    """The fused 2/3 path copies only the kept slabs of a host field: values outside the kept box
+    (NaN here) must not reach the result, which equals the clean field's and the oracle's."""
+    F.clear_plans()
+    u, ks = spectrum_field((64, 64, 64), e_config2, seed=7)
+    kw = dict(binning=F.LinearBinning(4.0), dealiasing=F.OrszagTwoThirds(), spectral=F.GB300Spectral(32),
+              execution=F.GB300Execution("batched"))
+    clean = F.calculate_shell_to_shell_transfer(u, ks, **kw).transfer_matrix
+    idx = np.arange(64)
+    kept = np.minimum(idx, 64 - idx) < 64 // 3
+    box = kept[:, None, None] & kept[None, :, None] & kept[None, None, :]
+    dirty = u.copy()
+    dirty[~box] = np.nan
+    got = F.calculate_shell_to_shell_transfer(dirty, ks, **kw).transfer_matrix
+    assert np.all(np.isfinite(got))
+    assert np.array_equal(got, clean)
+    _, _, T, _, _ = O.shell_to_shell(u, ks, ("linear", 4.0), "two_thirds")
+    assert rel(got, T) < 1e-5
