@@ -16,4 +16,15 @@ int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, c
   }
 }
 
+// Pencils per tile of the fused strided passes for transform length N (0 when not built here).
+int fz_tile_cols_a(int N) {
+  switch (N) {
+    case 64: return FzTile<64>::C;
+    case 128: return FzTile<128>::C;
+    case 256: return FzTile<256>::C;
+    case 512: return FzTile<512>::C;
+    default: return 0;
+  }
+}
+
 }  // namespace fit

@@ -16,4 +16,15 @@ int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, c
   }
 }
 
+// Pencils per tile of the fused strided passes for transform length N (0 when not built here).
+int fz_tile_cols_b(int N) {
+  switch (N) {
+    case 96: return FzTile<96>::C;
+    case 192: return FzTile<192>::C;
+    case 384: return FzTile<384>::C;
+    case 768: return FzTile<768>::C;
+    default: return 0;
+  }
+}
+
 }  // namespace fit

@@ -55,15 +55,29 @@ struct FzArgs {
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
 FIT_D float2 fz_muli(float2 h, float k) { return make_float2(-h.y * k, h.x * k); }   // i*k*h
 
+// Tile of the fused strided passes (zinv, yinv, yfwd, zfwd_bin): C pencils of N points, EPT
+// elements per thread; MINB resident blocks per SM bound the registers.
+template <int N>
+struct FzTile {
+  static constexpr int C = N == 512 ? 8 : CtTile<float2, N>::C;
+  static constexpr int E = C * N;
+  static constexpr int EPT = E <= 8192 ? 8 : 16;
+  static constexpr int NTHR = (E / EPT + 31) / 32 * 32;
+  static constexpr size_t SMEM = (size_t)(E + N) * 8;
+  static constexpr int MINB = N == 512 ? 4 : CtTile<float2, N>::MINB;
+  static constexpr int MINB_Y = MINB;     // yinv
+  static constexpr int MINB_BIN = MINB;   // zfwd_bin (per-thread transfer sums stay live across transforms)
+};
+
 // ---- zinv --------------------------------------------------------------------------------------
 // One block per (mediator, component and derivative, pencil tile): the tile's modes of the
 // mediator's shell are scattered from their list into a zeroed tile, then transformed along z.
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_zinv(FzArgs a, const float2* __restrict__ H,
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv(FzArgs a, const float2* __restrict__ H,
                                                                     const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
-  typedef CtTile<float2, N> TT;
+  typedef FzTile<N> TT;
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
   static_assert(C <= 64 && NT * EPT == E, "zinv: tile column must fit the list entry");
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
@@ -119,11 +133,11 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MI
 
 // ---- yinv --------------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_yinv(FzArgs a, const float2* __restrict__ in,
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(FzArgs a, const float2* __restrict__ in,
                                                                     const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
-  typedef CtTile<float2, N> TT;
+  typedef FzTile<N> TT;
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -160,12 +174,12 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MI
 
 // ---- xmix: inverse x transforms, product with the advecting velocity, forward x transform -----
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR) k_fz_xmix(FzArgs a, const float2* __restrict__ G,
+__global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const float2* __restrict__ G,
                                                                     const float* __restrict__ U,
                                                                     const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
-  typedef CtTile<float2, N> TT;
+  typedef FzTile<N> TT;
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
   static_assert(NT * EPT == E, "xmix needs an exact thread/element split");
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
@@ -552,10 +566,10 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
 
 // ---- yfwd --------------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
-  typedef CtTile<float2, N> TT;
+  typedef FzTile<N> TT;
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -588,12 +602,12 @@ __global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MI
 // rarely, so each thread keeps a running (shell, sum) pair and flushes it to the block's FP64
 // shared-memory bins only when the shell changes.
 template <int N>
-__global__ void __launch_bounds__(CtTile<float2, N>::NTHR, CtTile<float2, N>::MINB) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
                                                                         const float2* __restrict__ Ceff,
                                                                         const uint16_t* __restrict__ seff,
                                                                         double* __restrict__ partial,
                                                                         const float2* __restrict__ twg) {
-  typedef CtTile<float2, N> TT;
+  typedef FzTile<N> TT;
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
   static_assert(NT * EPT == E && (NT / C) * EPT == N, "zfwd needs an exact thread/element split");
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
@@ -706,7 +720,7 @@ template <int N>
 int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
              const float* kd, const float* U, float2* bufA, float2* bufB, double* partial, const float2* tw,
              int* err, cudaStream_t st) {
-  typedef CtTile<float2, N> TT;
+  typedef FzTile<N> TT;
   constexpr int C = TT::C;
   const size_t sm = TT::SMEM;
   const size_t smb = TT::SMEM + sizeof(double) * a.nsh + 16;

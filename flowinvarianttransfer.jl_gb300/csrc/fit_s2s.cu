@@ -17,6 +17,8 @@ namespace fit {
 int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
                   const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
                   const float2* tw, int* err, cudaStream_t st);
+int fz_tile_cols_a(int N);
+int fz_tile_cols_b(int N);
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
                   const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
                   const float2* tw, int* err, cudaStream_t st);
@@ -197,11 +199,6 @@ static bool fused_ok(const fit_plan* p) {
 // the mode (the set-up and gather kernels skip the masked modes' loads).
 int s2s_reads_kept_box(const fit_plan* p) { return fused_ok(p) && p->dealias == 1 ? 1 : 0; }
 
-static int ct_cols32(int N) {   // CtTile<float2, N>::C
-  int w = 1;
-  while (w * 2 <= 4096 / N) w *= 2;
-  return w > 16 ? w : 16;
-}
 
 // H (Hermitian part of the masked / embedded velocity), band shell, effective carrier and
 // binning shell for every live half-spectrum mode, compact layout [c][kz'][kx + KX ky']. CT is the
@@ -319,7 +316,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   const int K = (p->dealias == 1) ? N / 3 - 1 : N / 2;
   const int KX = K + 1, KY = 2 * K + 1;
   const long P1 = (long)KX * KY, L = (long)M * M;
-  const int C = ct_cols32(M);
+  const int C = fz_tile_cols_a(M) > 0 ? fz_tile_cols_a(M) : fz_tile_cols_b(M);
   const long npt = (P1 + C - 1) / C;
   const double perA = (double)(6.0 * M * P1 > 3.0 * L * KX ? 6.0 * M * P1 : 3.0 * L * KX);
   const double perB = (double)(9.0 * L * KX > 3.0 * M * P1 ? 9.0 * L * KX : 3.0 * M * P1);
