@@ -129,7 +129,9 @@ def prof_read_all():
     """{kind name: (ms_total, algorithmic_bytes_total, launches)} since the last prof_enable."""
     lib = load()
     out = {}
-    for k in range(14):
+    for k in range(64):
+        if not lib.fit_prof_kind_name(k):
+            break
         ms, by, n = C.c_double(), C.c_double(), C.c_longlong()
         check(lib.fit_prof_read(k, C.byref(ms), C.byref(by), C.byref(n)))
         if n.value:

@@ -27,4 +27,16 @@ int fz_tile_cols_a(int N) {
   }
 }
 
+// Self-advecting velocity in physical space over the live box (1 when N is not built here).
+int fz_velocity_a(int N, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U, const float2* tw,
+                   float scale, cudaStream_t st) {
+  switch (N) {
+    case 64: return fz_velocity<64>(a, H, bufZ, bufY, U, tw, scale, st);
+    case 128: return fz_velocity<128>(a, H, bufZ, bufY, U, tw, scale, st);
+    case 256: return fz_velocity<256>(a, H, bufZ, bufY, U, tw, scale, st);
+    case 512: return fz_velocity<512>(a, H, bufZ, bufY, U, tw, scale, st);
+    default: return 1;
+  }
+}
+
 }  // namespace fit

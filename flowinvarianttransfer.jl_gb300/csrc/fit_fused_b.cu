@@ -27,4 +27,16 @@ int fz_tile_cols_b(int N) {
   }
 }
 
+// Self-advecting velocity in physical space over the live box (1 when N is not built here).
+int fz_velocity_b(int N, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U, const float2* tw,
+                   float scale, cudaStream_t st) {
+  switch (N) {
+    case 96: return fz_velocity<96>(a, H, bufZ, bufY, U, tw, scale, st);
+    case 192: return fz_velocity<192>(a, H, bufZ, bufY, U, tw, scale, st);
+    case 384: return fz_velocity<384>(a, H, bufZ, bufY, U, tw, scale, st);
+    case 768: return fz_velocity<768>(a, H, bufZ, bufY, U, tw, scale, st);
+    default: return 1;
+  }
+}
+
 }  // namespace fit

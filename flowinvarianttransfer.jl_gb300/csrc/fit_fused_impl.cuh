@@ -668,6 +668,101 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
   for (int t = tid; t < a.nsh; t += NT) pb[(long)t * gridDim.z] = bins[t];
 }
 
+// ---- self-advecting velocity in physical space from H ------------------------------------------
+// U = real(ifft3(Herm part of the masked velocity)) over the live box only: z pass of the KX x KY
+// live pencils, y pass of the live kx columns, x pass two Hermitian lines per complex transform.
+// Layouts: H [c][kz'][col] -> [c][z][col] -> [c][z][y][kx] -> U [c][z][y][x].
+template <int N>
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uz(FzArgs a, const float2* __restrict__ H,
+                                                                          float2* __restrict__ out,
+                                                                          const float2* __restrict__ twg) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const long c0 = (long)blockIdx.y * C;
+  const int c = blockIdx.x;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  const float2* Hc = H + (long)c * a.KY * a.P1;
+  float2* oc = out + (long)c * N * a.P1;
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const long col = c0 + cc;
+        const int f = fz_freq(e, N);
+        return (col < a.P1 && f >= -a.K && f <= a.K) ? Hc[(long)(f + a.K) * a.P1 + col] : make_float2(0.f, 0.f);
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const long col = c0 + cc;
+        if (col < a.P1) oc[(long)e * a.P1 + col] = val;
+      });
+}
+
+template <int N>
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uy(FzArgs a, const float2* __restrict__ in,
+                                                                          float2* __restrict__ out,
+                                                                          const float2* __restrict__ twg) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const int nkt = (a.KX + C - 1) / C;
+  const int z = blockIdx.y / nkt, k0 = (blockIdx.y % nkt) * C, c = blockIdx.x;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  const float2* ib = in + ((long)c * N + z) * a.P1;
+  float2* ob = out + ((long)c * N + z) * N * a.KX;
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const int kx = k0 + cc;
+        const int f = fz_freq(e, N);
+        return (kx < a.KX && f >= -a.K && f <= a.K) ? ib[kx + (long)a.KX * (f + a.K)] : make_float2(0.f, 0.f);
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const int kx = k0 + cc;
+        if (kx < a.KX) ob[(long)e * a.KX + kx] = val;
+      });
+}
+
+template <int N>
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_ux(FzArgs a, const float2* __restrict__ in,
+                                                                          float* __restrict__ out,
+                                                                          const float2* __restrict__ twg, float scale) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const long l0 = (long)blockIdx.x * 2 * C;   // lines of all three components, 2C per block
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int k, int col) -> float2 {
+        const bool cj = 2 * k > N;
+        const int kk = cj ? N - k : k;
+        float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+        if (kk <= a.K) {   // |kx| <= K < N / 2: the self-conjugate bin N / 2 never holds data
+          A = in[(l0 + 2 * col) * a.KX + kk];
+          B = in[(l0 + 2 * col + 1) * a.KX + kk];
+          if (cj) { A.y = -A.y; B.y = -B.y; }
+          if (k == 0) { A.y = 0.f; B.y = 0.f; }
+        }
+        return make_float2(A.x - B.y, A.y + B.x);
+      },
+      [&](int, int, int x, int col, float2 zv) {
+        out[(l0 + 2 * col) * N + x] = zv.x * scale;
+        out[(l0 + 2 * col + 1) * N + x] = zv.y * scale;
+      });
+}
+
 // Raise the dynamic shared-memory limit and size the carveout for the kernel's occupancy.
 template <typename K>
 static int ct_prep_fused(K kern, size_t smem, int nthr) {
@@ -713,6 +808,34 @@ static int fz_xpair(int KX, int C) {
     if (hits < best_hits) best_hits = hits, best = mode;
   }
   return best;
+}
+
+// ---- host launcher of the velocity passes (instantiated per transform length) --------------------
+// bufZ holds 3 N P1 and bufY 3 N^2 KX complex values; U receives 3 N^3 floats scaled by `scale`.
+template <int N>
+int fz_velocity(const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U, const float2* tw, float scale,
+                cudaStream_t st) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C;
+  FIT_TRY(ct_prep_fused(k_fz_uz<N>, TT::SMEM, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_uy<N>, TT::SMEM, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_ux<N>, TT::SMEM, TT::NTHR));
+  const unsigned pt = (unsigned)((a.P1 + C - 1) / C);
+  const unsigned nkt = (unsigned)((a.KX + C - 1) / C);
+  const double cpx = 8.0, L = (double)N * N;
+  fit_prof_begin(PK_S2S_VELOCITY, cpx * 3.0 * (a.KY + (double)N) * a.P1, st);
+  k_fz_uz<N><<<dim3(3, pt), TT::NTHR, TT::SMEM, st>>>(a, H, bufZ, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_VELOCITY, cpx * 3.0 * ((double)N * a.P1 + L * a.KX), st);
+  k_fz_uy<N><<<dim3(3, nkt * N), TT::NTHR, TT::SMEM, st>>>(a, bufZ, bufY, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_VELOCITY, 3.0 * L * (cpx * a.KX + 4.0 * N), st);
+  k_fz_ux<N><<<(unsigned)(3 * a.L / (2 * C)), TT::NTHR, TT::SMEM, st>>>(a, bufY, U, tw, scale);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
 }
 
 // ---- host launcher for one batch (instantiated per transform length) -------------------------

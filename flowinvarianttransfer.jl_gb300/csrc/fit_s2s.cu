@@ -17,6 +17,10 @@ namespace fit {
 int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
                   const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
                   const float2* tw, int* err, cudaStream_t st);
+int fz_velocity_a(int N, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U, const float2* tw,
+                  float scale, cudaStream_t st);
+int fz_velocity_b(int N, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U, const float2* tw,
+                  float scale, cudaStream_t st);
 int fz_tile_cols_a(int N);
 int fz_tile_cols_b(int N);
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
@@ -339,7 +343,6 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     FIT_TRY(ensure(p, &s->ferr, sizeof(int)));
     FIT_CUDA_CHECK(cudaMemset(s->ferr.p, 0, sizeof(int)));
   }
-  FIT_TRY(ensure(p, &p->hs, sizeof(float2) * 3 * g.Mhalf));
   FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
   if (s->fkd_n != KY) {   // derivative multipliers of the live indices (never during capture)
     std::vector<float> kd(KY);
@@ -389,21 +392,6 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     s->zl_f32 = p->cached_f32;
     s->zl_nsh = nsh;
   }
-  // advecting velocity in physical space (once per call)
-  GatherArgs ga;
-  memset(&ga, 0, sizeof(ga));
-  ga.src[0] = ud;
-  ga.src[1] = ad;
-  ga.src_comp_stride[0] = g.Ntot;
-  ga.src_comp_stride[1] = g.Ntot;
-  ga.in_f64 = p->io_f64;
-  ga.two_thirds = p->dealias == 1;
-  ga.scale = 1.0;
-  ga.nfields = 3;
-  for (int j = 0; j < 3; ++j) ga.f[j] = GatherField{1, j, -1, 0};
-  FIT_TRY(gather_half<float>(g, p->kt, ga, (float2*)p->hs.p, p->stream));
-  FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)(1.0 / (double)g.Mtot),
-                            p->stream));
   FzArgs a;
   memset(&a, 0, sizeof(a));
   a.K = K;
@@ -418,6 +406,29 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   a.zent = (const uint16_t*)s->zent.p;
   a.ntile = ntile;
   const float2* tw = p->ax[0].tw32;
+  // advecting velocity in physical space (once per call)
+  if (ad == ud) {   // self-advection: H already holds its live box
+    const float sc = (float)(1.0 / (double)g.Mtot);
+    int rc = fz_velocity_a(M, a, H, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p, tw, sc, p->stream);
+    if (rc == 1) rc = fz_velocity_b(M, a, H, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p, tw, sc, p->stream);
+    if (rc != FIT_OK) return rc == 1 ? FIT_ERR_SIZE : rc;
+  } else {
+    FIT_TRY(ensure(p, &p->hs, sizeof(float2) * 3 * g.Mhalf));
+    GatherArgs ga;
+    memset(&ga, 0, sizeof(ga));
+    ga.src[0] = ud;
+    ga.src[1] = ad;
+    ga.src_comp_stride[0] = g.Ntot;
+    ga.src_comp_stride[1] = g.Ntot;
+    ga.in_f64 = p->io_f64;
+    ga.two_thirds = p->dealias == 1;
+    ga.scale = 1.0;
+    ga.nfields = 3;
+    for (int j = 0; j < 3; ++j) ga.f[j] = GatherField{1, j, -1, 0};
+    FIT_TRY(gather_half<float>(g, p->kt, ga, (float2*)p->hs.p, p->stream));
+    FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)(1.0 / (double)g.Mtot),
+                              p->stream));
+  }
   for (size_t b0 = 0; b0 < meds.size(); b0 += B) {
     a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
     for (int b = 0; b < a.nb; ++b) {
