@@ -11,8 +11,8 @@
 // pass (no N_m field is written):
 //
 //   zinv  : z pass of H * [shell == m] and of ik_z * H * [shell == m]        (6 outputs / m)
-//   yinv  : y pass -> Y(P), Y(ik_y P), Y(Q)   (P, Q = the two zinv outputs)   (9 outputs / m)
-//   xmix  : per component c: sum_j u_j * C2R(ik_x? G_cj) -> R2C -> kx <= K     (3 outputs / m)
+//   yinv  : y pass -> Y(ik_x P), Y(ik_y P), Y(Q)   (P, Q = the two zinv outputs) (9 outputs / m)
+//   xmix  : per component c: sum_j u_j * C2R(G_cj) -> R2C -> kx <= K           (3 outputs / m)
 //   yfwd  : y pass forward, keep ky in [-K, K]                                 (3 outputs / m)
 //   zfwd  : z pass forward, t = sum_c Re(conj(Ceff_c) N_c), FP64 shell bins per block
 //
@@ -163,6 +163,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
           const int ky = f + a.K;
           val = in[ib + kx + (long)a.KX * ky];
           if (j == 1) val = fz_muli(val, kd[ky]);
+          if (j == 0) val = fz_muli(val, kd[a.K + kx]);   // x derivative of the j = 0 output
         }
         return val;
       },
@@ -176,7 +177,6 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
 template <int N>
 __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const float2* __restrict__ G,
                                                                     const float* __restrict__ U,
-                                                                    const float* __restrict__ kd,
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
@@ -209,11 +209,6 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const flo
         if (kk <= ex) {
           if (la < a.L) A = G[(gb + la) * a.KX + kk];
           if (lb < a.L) B = G[(gb + lb) * a.KX + kk];
-          if (j == 0) {
-            const float kx = kd[a.K + kk];
-            A = fz_muli(A, kx);
-            B = fz_muli(B, kx);
-          }
           if (cj) { A.y = -A.y; B.y = -B.y; }
           if (k == 0) { A.y = 0.f; B.y = 0.f; }
         }
@@ -276,7 +271,6 @@ struct XTile {
 template <int N>
 __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, const float2* __restrict__ G,
                                                                 const float* __restrict__ U,
-                                                                const float* __restrict__ kd,
                                                                 float2* __restrict__ out,
                                                                 const float2* __restrict__ twg, int* err) {
   typedef XTile<N> TT;
@@ -352,11 +346,6 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
           if (kk <= ex) {
             A = sg[(2 * col) * a.KX + kk];
             B = sg[(2 * col + 1) * a.KX + kk];
-            if (j == 0) {
-              const float kx = kd[a.K + kk];
-              A = fz_muli(A, kx);
-              B = fz_muli(B, kx);
-            }
             if (cj) { A.y = -A.y; B.y = -B.y; }
             if (k == 0) { A.y = 0.f; B.y = 0.f; }
           }
@@ -426,7 +415,6 @@ struct XRTile {
 template <int N>
 __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, const float2* __restrict__ G,
                                                                 const float* __restrict__ U,
-                                                                const float* __restrict__ kd,
                                                                 float2* __restrict__ out,
                                                                 const float2* __restrict__ twg, int* err) {
   typedef XRTile<N> TT;
@@ -510,11 +498,6 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
             const int ra = xp ? col : 2 * col, rb = xp ? col + C : 2 * col + 1;
             A = sg[ra * a.KX + kk];
             B = sg[rb * a.KX + kk];
-            if (j == 0) {
-              const float kx = kd[a.K + kk];
-              A = fz_muli(A, kx);
-              B = fz_muli(B, kx);
-            }
             if (cj) { A.y = -A.y; B.y = -B.y; }
             if (k == 0) { A.y = 0.f; B.y = 0.f; }
           }
@@ -889,17 +872,17 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
         FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
         FzArgs ax = a;
         ax.xpair = fz_xpair(a.KX, XR::C);
-        k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, bufB, U, kd, bufA,
+        k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, bufB, U, bufA,
                                                                                               tw, err);
       }
     }
     if (reg) {
     } else if (bulk) {
       FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx, XT::NTHR));
-      k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, bufB, U, kd, bufA, tw,
+      k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, bufB, U, bufA, tw,
                                                                                              err);
     } else {
-      k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, sm, st>>>(a, bufB, U, kd, bufA,
+      k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, sm, st>>>(a, bufB, U, bufA,
                                                                                                 tw);
     }
   }
