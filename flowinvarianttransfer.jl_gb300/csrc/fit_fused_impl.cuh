@@ -456,14 +456,13 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
     mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
     for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + urow(r) * TT::UP, U + (l0 + r) * N, (uint32_t)(N * 4), &bar[2]);
   }
-  // after a timed-out wait: give the copies this block still has in flight a bounded chance to
-  // land before the block exits (gradient tiles t and t+1, velocity tile t)
-  auto drain = [&](int t, bool g_done, bool u_done) {
-    if (tid != 0) return;
-    if (!g_done) mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1), 200000000LL);
-    if (t + 1 < 9) mbar_wait_bounded(&bar[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1), 200000000LL);
-    if (!u_done) mbar_wait_bounded(&bar[2], (uint32_t)(t & 1), 200000000LL);
-  };
+  // Every thread waits on the copy barriers itself (the completed phase makes the bulk-copied data
+  // visible to it), so no block barrier is spent on the waits. A wait that runs out marks this
+  // thread failed and the block carries on with whatever the tile holds (indices never depend on
+  // data, so every access stays in bounds and every thread reaches the same barriers); the flag
+  // tells the host to discard the result. Thread 0 waits on every phase too and stops issuing
+  // copies once one of its own waits failed, so every later wait is bounded as well.
+  bool failed = false;
   float2 acc[MB][RL];
   for (int t = 0; t < 9; ++t) {
     const int c = t / 3, j = t % 3, buf = t & 1;
@@ -473,22 +472,17 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
 #pragma unroll
         for (int q = 0; q < RL; ++q) acc[i][q] = make_float2(0.f, 0.f);
     }
-    if (tid == 0 && t + 1 < 9) {
+    if (tid == 0 && t + 1 < 9 && !failed) {   // after a failed wait, issue nothing more
       const int c1 = (t + 1) / 3, j1 = (t + 1) % 3, nb1 = (t + 1) & 1;
       const long gb = (((long)b * 3 + c1) * 3 + j1) * a.L;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[nb1], gbytes);
       bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KX, gbytes, &bar[nb1]);
     }
-    const bool okg = mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL);
-    if (__syncthreads_or(!okg)) {
-      if (tid == 0) atomicExch(err, 1);
-      drain(t, false, false);
-      return;
-    }
+    if (!mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL)) failed = true;
     const float2* sg = stg + buf * SB;
     const float sp = a.sp;
-    const bool ok = ct_fft_mapped_mid<float2, true, N, C, NT, EPT>(
+    ct_fft_mapped_mid<float2, true, N, C, NT, EPT>(
         s, tw, tid,
         [&](int, int, int k, int col) -> float2 {
           const bool cj = 2 * k > N;
@@ -504,20 +498,15 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           return make_float2(A.x - B.y, A.y + B.x);
         },
         [&]() -> bool {   // the velocity tile of this j must have landed before the last stage
-          const bool oku = mbar_wait_bounded(&bar[2], (uint32_t)(t & 1), 2000000000LL);
-          return !__syncthreads_or(!oku);
+          if (!mbar_wait_bounded(&bar[2], (uint32_t)(t & 1), 2000000000LL)) failed = true;
+          return true;
         },
         [&](int i, int q, int x, int col, float2 zv) {
           acc[i][q].x += us[col * TT::UP + x] * (zv.x * sp);
           acc[i][q].y += us[(col + C) * TT::UP + x] * (zv.y * sp);
         });
-    if (!ok) {
-      if (tid == 0) atomicExch(err, 1);
-      drain(t, true, false);
-      return;
-    }
     __syncthreads();   // s and the velocity tile are free
-    if (tid == 0 && t + 1 < 9) {
+    if (tid == 0 && t + 1 < 9 && !failed) {   // after a failed wait, issue nothing more
       const int j1 = (t + 1) % 3;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
@@ -544,6 +533,12 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
       }
       __syncthreads();
     }
+  }
+  if (failed) atomicExch(err, 1);
+  if (tid == 0) {   // no copy may still be landing when the block exits: final phases 4, 3, 8
+    mbar_wait_bounded(&bar[0], 0u, 200000000LL);
+    mbar_wait_bounded(&bar[1], 1u, 200000000LL);
+    mbar_wait_bounded(&bar[2], 0u, 200000000LL);
   }
 }
 
