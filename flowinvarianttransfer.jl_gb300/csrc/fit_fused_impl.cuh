@@ -42,7 +42,6 @@ struct FzArgs {
   int nb;       // mediators in this launch
   int med[16];  // their shell numbers (1-based)
   short ext[16][3];   // per mediator: largest |signed frequency| of its shell's modes along x, y, z
-  float sp;     // 1 / Mtot (physical-space normalisation of the inverse transforms)
   float so;     // output normalisation of the forward transform (1/Ntot, or Mtot/Ntot^2 padded)
   int xpair;    // x pass: complex column c carries lines (2c, 2c+1) (0) or (c, c+C) (1) of its tile
   // z pass inputs as lists: the modes of band shell m in pencil tile t (C consecutive pencils) are
@@ -225,8 +224,8 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const flo
         const float2 zv = s[swz(x, col, C)];
         const float ua = (la < a.L) ? Uj[la * N + x] : 0.f;
         const float ub = (lb < a.L) ? Uj[lb * N + x] : 0.f;
-        acc[r].x += ua * (zv.x * a.sp);
-        acc[r].y += ub * (zv.y * a.sp);
+        acc[r].x += ua * zv.x;
+        acc[r].y += ub * zv.y;
       }
     }
     __syncthreads();
@@ -358,8 +357,8 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
       const int i = tid + r * NT;
       const int col = i / N, x = i % N;
       const float2 zv = s[swz(x, col, C)];
-      acc[r].x += ua[r] * (zv.x * a.sp);
-      acc[r].y += ub[r] * (zv.y * a.sp);
+      acc[r].x += ua[r] * zv.x;
+      acc[r].y += ub[r] * zv.y;
     }
     __syncthreads();
     if (j == 2) {
@@ -481,7 +480,6 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
     }
     if (!mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL)) failed = true;
     const float2* sg = stg + buf * SB;
-    const float sp = a.sp;
     ct_fft_mapped_mid<float2, true, N, C, NT, EPT>(
         s, tw, tid,
         [&](int, int, int k, int col) -> float2 {
@@ -502,8 +500,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           return true;
         },
         [&](int i, int q, int x, int col, float2 zv) {
-          acc[i][q].x += us[col * TT::UP + x] * (zv.x * sp);
-          acc[i][q].y += us[(col + C) * TT::UP + x] * (zv.y * sp);
+          acc[i][q].x += us[col * TT::UP + x] * zv.x;
+          acc[i][q].y += us[(col + C) * TT::UP + x] * zv.y;
         });
     __syncthreads();   // s and the velocity tile are free
     if (tid == 0 && t + 1 < 9 && !failed) {   // after a failed wait, issue nothing more

@@ -400,15 +400,17 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   a.P1 = P1;
   a.L = L;
   a.nsh = nsh;
-  a.sp = (float)(1.0 / (double)g.Mtot);
   a.so = (float)(g.padded ? (double)g.Mtot / ((double)g.Ntot * (double)g.Ntot) : 1.0 / (double)g.Ntot);
   a.zoff = (const unsigned*)s->zoff.p;
   a.zent = (const uint16_t*)s->zent.p;
   a.ntile = ntile;
   const float2* tw = p->ax[0].tw32;
-  // advecting velocity in physical space (once per call)
+  // advecting velocity in physical space (once per call), its unnormalised inverse transform scaled
+  // by 1/Mtot^2: the x pass multiplies it by the unnormalised inverse transforms of the gradients,
+  // so that product carries both transforms' 1/Mtot without a per-element rescale
+  const double usc = 1.0 / ((double)g.Mtot * (double)g.Mtot);
   if (ad == ud) {   // self-advection: H already holds its live box
-    const float sc = (float)(1.0 / (double)g.Mtot);
+    const float sc = (float)usc;
     int rc = fz_velocity_a(M, a, H, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p, tw, sc, p->stream);
     if (rc == 1) rc = fz_velocity_b(M, a, H, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p, tw, sc, p->stream);
     if (rc != FIT_OK) return rc == 1 ? FIT_ERR_SIZE : rc;
@@ -426,8 +428,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     ga.nfields = 3;
     for (int j = 0; j < 3; ++j) ga.f[j] = GatherField{1, j, -1, 0};
     FIT_TRY(gather_half<float>(g, p->kt, ga, (float2*)p->hs.p, p->stream));
-    FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)(1.0 / (double)g.Mtot),
-                              p->stream));
+    FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)usc, p->stream));
   }
   for (size_t b0 = 0; b0 < meds.size(); b0 += B) {
     a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
