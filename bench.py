@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--dk", type=float, default=14.0)
     ap.add_argument("--seed", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial", "padded", "m2m"],
