@@ -133,8 +133,9 @@ FIT_D void mlp_tile_forward(const MlpSmem* w, const uint32_t* xa, uint32_t h1a[4
 // the network sees the direction of the gradient tensor and its output is multiplied by s, so the
 // predicted stress is homogeneous of degree 2 in A, like the exact subfilter stress at leading
 // order (tau ~ ell^2/12 A A^T for a Gaussian filter).
+// raw (optional): the unscaled features this lane loaded, [row][col group][pair].
 FIT_D void mlp_load_x(const float* __restrict__ X, long ld, long P, long p0, const float* sc, uint32_t* xa,
-                      int lane, bool homog, float* s) {
+                      int lane, bool homog, float* s, float (*raw)[2][2] = nullptr) {
   const int g = lane >> 2, t = lane & 3;
   float v[2][2][2];   // [row g / g+8][col group 2t / 2t+8][pair]
 #pragma unroll
@@ -145,7 +146,9 @@ FIT_D void mlp_load_x(const float* __restrict__ X, long ld, long P, long p0, con
       for (int e = 0; e < 2; ++e) {
         const int f = 2 * t + 8 * cg + e;
         const long p = p0 + g + 8 * r;
-        v[r][cg][e] = (f < 9 && p < P) ? X[(long)f * ld + p] * sc[f] : 0.f;
+        const float x = (f < 9 && p < P) ? X[(long)f * ld + p] : 0.f;
+        if (raw) raw[r][cg][e] = x;
+        v[r][cg][e] = x * sc[f < 9 ? f : 0];
       }
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
@@ -167,6 +170,33 @@ FIT_D void mlp_load_x(const float* __restrict__ X, long ld, long P, long p0, con
   xa[3] = pack_bf16(v[1][1][0], v[1][1][1]);
 }
 
+// The nine features of the point of row r, gathered from the quad of lanes that loaded them
+// (lane t holds features 2t, 2t+1 and, for t = 0, feature 8).
+FIT_D void quad_features(const float (*raw)[2][2], int r, int lane, float* A) {
+  const int q0 = lane & ~3;
+#pragma unroll
+  for (int f = 0; f < 8; ++f) {
+    const float mine = (f & 1) ? raw[r][0][1] : raw[r][0][0];
+    A[f] = __shfl_sync(0xffffffffu, mine, q0 | (f >> 1));
+  }
+  A[8] = __shfl_sync(0xffffffffu, raw[r][1][0], q0);
+}
+
+// Gradient-model stress (below) and Pi = -tau_ij S_ij, S = (A + A^T)/2 (the closure's flux, fused
+// epilogue), on a point's features held in registers.
+FIT_D float gradient_model_stress_r(int o, const float* A) {
+  const int i = o < 3 ? o : (o == 5 ? 1 : 0), j = o < 3 ? o : (o == 3 ? 1 : 2);
+  float t = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) t += A[3 * i + k] * A[3 * j + k];
+  return t;
+}
+FIT_D float stress_dot_strain_r(int o, float tau, const float* A) {
+  const int i = o < 3 ? o : (o == 5 ? 1 : 0), j = o < 3 ? o : (o == 3 ? 1 : 2);
+  if (i == j) return -tau * A[3 * i + i];
+  return -tau * (A[3 * i + j] + A[3 * j + i]);
+}
+
 // Gradient-model stress component o (00 11 22 01 02 12) without its ell^2/12 factor: sum_k A_ik A_jk.
 FIT_D float gradient_model_stress(int o, const float* __restrict__ X, long ld, long p) {
   const int i = o < 3 ? o : (o == 5 ? 1 : 0), j = o < 3 ? o : (o == 3 ? 1 : 2);
@@ -174,13 +204,6 @@ FIT_D float gradient_model_stress(int o, const float* __restrict__ X, long ld, l
 #pragma unroll
   for (int k = 0; k < 3; ++k) t += X[(long)(3 * i + k) * ld + p] * X[(long)(3 * j + k) * ld + p];
   return t;
-}
-
-// Pi = -tau_ij S_ij of the predicted stress, S = (A + A^T)/2 (the closure's flux, fused epilogue).
-FIT_D float stress_dot_strain(int o, float tau, const float* __restrict__ X, long ld, long p) {
-  const int i = o < 3 ? o : (o == 5 ? 1 : 0), j = o < 3 ? o : (o == 3 ? 1 : 2);
-  if (i == j) return -tau * X[(long)(3 * i + i) * ld + p];
-  return -tau * (X[(long)(3 * i + j) * ld + p] + X[(long)(3 * j + i) * ld + p]);
 }
 
 __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ Pm, const float* __restrict__ X,
@@ -199,21 +222,23 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ P
   for (long tile = (long)blockIdx.x * nw + warp; tile < ntile; tile += (long)gridDim.x * nw) {
     const long p0 = tile * 16;
     uint32_t xa[4], h1a[4][4], h2a[4][4];
-    float y[4], sn[2];
-    mlp_load_x(X, ld, P, p0, sc, xa, lane, homog != 0, sn);
+    float y[4], sn[2], raw[2][2][2];
+    mlp_load_x(X, ld, P, p0, sc, xa, lane, homog != 0, sn, raw);
     mlp_tile_forward(&w, xa, h1a, h2a, y, lane);
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
       const long p = p0 + g + 8 * r;
+      float A[9];
+      quad_features(raw, r, lane, A);
       float part = 0.f;
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
         const int o = 2 * t + e;
         if (o < 6 && p < P) {
           float tau = y[2 * r + e] * sn[r] * osc[o];
-          if (clark != 0.f) tau += clark * gradient_model_stress(o, X, ld, p);
+          if (clark != 0.f) tau += clark * gradient_model_stress_r(o, A);
           if (Y) Y[(long)o * ld + p] = tau;
-          if (Pi) part += stress_dot_strain(o, tau, X, ld, p);
+          if (Pi) part += stress_dot_strain_r(o, tau, A);
         }
       }
       // the four lanes of a quad hold the six outputs of point p
