@@ -14,7 +14,7 @@ EXPORTS = [
     "fit_launch_count", "fit_nonlinear_term", "fit_assign_shells", "fit_transfer_density",
     "fit_spectral_flux", "fit_shell_to_shell", "fit_helical_decompose", "fit_helmholtz_decompose",
     "fit_partial_fluxes", "fit_mode_to_mode", "fit_prof_enable", "fit_prof_read", "fit_prof_kind_name",
-    "fit_coarse_graining_flux", "fit_forward_spectrum", "fit_ns_evolve", "fit_mlp_nparams", "fit_mlp_forward",
+    "fit_coarse_graining_flux", "fit_forward_spectrum", "fit_ns_evolve", "fit_mlp_nparams", "fit_mlp_forward", "fit_mlp_status",
     "fit_mlp_train_grad", "fit_mlp_adam", "fit_gradient_model_flux", "fit_field_moments", "fit_field_compare",
     "fit_batch_create", "fit_batch_destroy", "fit_batch_add_flux", "fit_batch_run", "fit_batch_run_eager", "fit_batch_info",
     "fit_autotune_enable", "fit_autotune_clear", "fit_autotune_info", "fit_autotune_entry",
@@ -61,6 +61,7 @@ def _declare(lib):
     lib.fit_forward_spectrum.argtypes = [vp, vp, vp, i32]
     lib.fit_ns_evolve.argtypes = [vp, vp, i32, C.c_double, C.c_double, C.c_double, C.c_double, i32]
     lib.fit_mlp_nparams.argtypes = []
+    lib.fit_mlp_status.argtypes = [C.POINTER(i32)]
     lib.fit_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp, i32, C.c_double, vp, vp, vp]
     lib.fit_stress_residual.argtypes = [vp, vp, i64, i64, C.c_double, vp, vp]
     lib.fit_mlp_train_grad.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, i32, vp, vp, vp]
@@ -119,6 +120,13 @@ def check(rc: int):
 
 def launch_count() -> int:
     return int(load().fit_launch_count())
+
+
+def mlp_status() -> int:
+    """1 when a clock-bounded wait inside an earlier MLP forward gave up (clears the flag)."""
+    v = C.c_int(0)
+    check(load().fit_mlp_status(C.byref(v)))
+    return int(v.value)
 
 
 def prof_enable(on: bool):

@@ -16,8 +16,10 @@
 // of the next layer's k16 step, so the forward pass chains layers in registers.
 #include <cuda_bf16.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "fit_common.cuh"
+#include "fit_umma.cuh"
 
 #define MLP_IN 16
 #define MLP_H 64
@@ -247,6 +249,161 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ P
       if (Pi && t == 0 && p < P) Pi[p] = part;
     }
   }
+}
+
+// ---- forward on the fifth-generation tensor cores (tcgen05) ---------------------------------------
+// One CTA of 128 threads handles 128 points per tile, one point per thread (tensor-memory lane =
+// thread). Each layer is D = A * W^T with M = 128: the A tile (BF16, canonical K-major layout) is
+// written to shared memory by the threads, thread 0 issues the MMAs (K = 16 steps) and commits
+// them to an mbarrier, every thread waits on it (clock-bounded) and reads its accumulator row from
+// tensor memory. Layer widths: 16 (9 features) -> 64 -> 64 -> 16 (6 outputs). The 64 tensor-memory
+// columns are reused by all three layers (each accumulator is read out before the next MMA).
+struct MlpTcSmem {
+  __nv_bfloat16 W1[64 * 16], W2[64 * 64], W3[16 * 64], A1[128 * 16], A2[128 * 64];   // canonical layouts
+  float b1[64], b2[64], b3[8], sc[9], osc[6];
+  uint64_t bar;
+  uint32_t tmem;
+};
+
+FIT_D void st_chunk(__nv_bfloat16* tile, uint32_t off, const float* v) {   // 8 BF16 values, 16 bytes
+  *reinterpret_cast<uint4*>(reinterpret_cast<char*>(tile) + off) =
+      make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+}
+
+FIT_D void st_bf16_at(__nv_bfloat16* tile, uint32_t off, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(tile) + off) = __float2bfloat16_rn(v);
+}
+
+// relu(D + b) of this thread's 64-column accumulator row -> its row of the next layer's A tile.
+FIT_D void hidden_to_a(uint32_t tl, const float* b, __nv_bfloat16* A2, int row) {
+#pragma unroll
+  for (int c4 = 0; c4 < 4; ++c4) {
+    float d[16];
+    tmem_ld16(tl + 16 * c4, d);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) d[i] = fmaxf(d[i] + b[16 * c4 + i], 0.f);
+    st_chunk(A2, umma_off(row, 16 * c4, 64), d);
+    st_chunk(A2, umma_off(row, 16 * c4 + 8, 64), d + 8);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict__ Pm, const float* __restrict__ X,
+                                                        long ld, long P, const float* __restrict__ in_scale,
+                                                        const float* __restrict__ t_scale, float* __restrict__ Y,
+                                                        float* __restrict__ Pi, int homog, float clark, int* err) {
+  extern __shared__ __align__(128) unsigned char mlp_tc_raw[];
+  MlpTcSmem& S = *reinterpret_cast<MlpTcSmem*>(mlp_tc_raw);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < 64 * 16; i += 128) st_bf16_at(S.W1, umma_off(i / 16, i % 16, 16), Pm[MlpOff::W1 + i]);
+  for (int i = tid; i < 64 * 64; i += 128) st_bf16_at(S.W2, umma_off(i / 64, i % 64, 64), Pm[MlpOff::W2 + i]);
+  for (int i = tid; i < 16 * 64; i += 128)   // outputs padded 8 -> 16 rows (rows 6.. never read out)
+    st_bf16_at(S.W3, umma_off(i / 64, i % 64, 64), i < 8 * 64 ? Pm[MlpOff::W3 + i] : 0.f);
+  if (tid < 64) {
+    S.b1[tid] = Pm[MlpOff::B1 + tid];
+    S.b2[tid] = Pm[MlpOff::B2 + tid];
+  }
+  if (tid < 8) S.b3[tid] = Pm[MlpOff::B3 + tid];
+  if (tid < 9) S.sc[tid] = in_scale[tid];
+  if (tid < 6) S.osc[tid] = 1.f / t_scale[tid];
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    mbar_init_fence();
+  }
+  if (warp == 0) {
+    tmem_alloc(&S.tmem, 64);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();   // weights written by the threads, read by the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tmem;
+  const uint32_t tl = tbase + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+  const uint32_t aA1 = smem_u32(S.A1), aA2 = smem_u32(S.A2);
+  const uint32_t aW1 = smem_u32(S.W1), aW2 = smem_u32(S.W2), aW3 = smem_u32(S.W3);
+  constexpr uint32_t ID64 = umma_idesc_bf16(128, 64), ID16 = umma_idesc_bf16(128, 16);
+  uint32_t phase = 0;
+  bool failed = false;
+  auto wait_mma = [&]() {
+    if (!mbar_wait_bounded(&S.bar, phase, 2000000000LL)) failed = true;
+    phase ^= 1u;
+    tc_fence_after();
+  };
+  auto publish_a = [&]() {   // A tile rows written by the threads -> visible to the MMA issue
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+  };
+  const long ntile = (P + 127) / 128;
+  for (long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const long p = tile * 128 + tid;
+    const bool live = p < P;
+    float A[9], v[16];
+#pragma unroll
+    for (int f = 0; f < 9; ++f) A[f] = live ? X[(long)f * ld + p] : 0.f;
+    float q = 0.f;
+#pragma unroll
+    for (int f = 0; f < 16; ++f) {
+      v[f] = f < 9 ? A[f] * S.sc[f] : 0.f;
+      q += v[f] * v[f];
+    }
+    const float sn = homog ? q : 1.f;
+    if (homog) {   // the network sees the direction of the scaled gradient tensor
+      const float inv = q > 0.f ? 1.f / sqrtf(q) : 0.f;
+#pragma unroll
+      for (int f = 0; f < 16; ++f) v[f] *= inv;
+    }
+    st_chunk(S.A1, umma_off(tid, 0, 16), v);
+    st_chunk(S.A1, umma_off(tid, 8, 16), v + 8);
+    publish_a();
+    if (tid == 0) {
+      tc_fence_after();
+      umma_bf16(tbase, umma_desc(aA1, 128, 256), umma_desc(aW1, 128, 256), ID64, false);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    hidden_to_a(tl, S.b1, S.A2, tid);
+    publish_a();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+        umma_bf16(tbase, umma_desc(aA2 + 256 * s, 128, 1024), umma_desc(aW2 + 256 * s, 128, 1024), ID64, s > 0);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    hidden_to_a(tl, S.b2, S.A2, tid);   // layer 2 has read A2: its MMAs completed
+    publish_a();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+        umma_bf16(tbase, umma_desc(aA2 + 256 * s, 128, 1024), umma_desc(aW3 + 256 * s, 128, 1024), ID16, s > 0);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    float y[16];
+    tmem_ld16(tl, y);
+    if (live) {
+      float part = 0.f;
+#pragma unroll
+      for (int o = 0; o < 6; ++o) {
+        float tau = (y[o] + S.b3[o]) * sn * S.osc[o];
+        if (clark != 0.f) tau += clark * gradient_model_stress_r(o, A);
+        if (Y) Y[(long)o * ld + p] = tau;
+        part += stress_dot_strain_r(o, tau, A);
+      }
+      if (Pi) Pi[p] = part;
+    }
+    tc_fence_before();
+    __syncthreads();   // accumulator columns and the A tiles are free for the next tile
+    tc_fence_after();
+  }
+  if (failed) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tbase, 64);
 }
 
 // ---- training: fused forward + backward, weight gradients reduced over points by MMAs --------------
@@ -552,7 +709,23 @@ __global__ void k_compare(const float* __restrict__ a, const float* __restrict__
 
 using namespace fit;
 
+static int* g_mlp_err = nullptr;
+
 extern "C" int fit_mlp_nparams(void) { return MLP_NPARAM; }
+
+// Reads and clears the tcgen05 forward's wait-timeout flag (synchronises the device): 0 when every
+// bounded wait of every earlier forward finished.
+extern "C" int fit_mlp_status(int* timed_out) {
+  if (!timed_out) {
+    fit_set_error("NULL argument");
+    return FIT_ERR_ARG;
+  }
+  *timed_out = 0;
+  if (!g_mlp_err) return FIT_OK;
+  FIT_CUDA_CHECK(cudaMemcpy(timed_out, g_mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
+  FIT_CUDA_CHECK(cudaMemset(g_mlp_err, 0, sizeof(int)));
+  return FIT_OK;
+}
 
 extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
                                const float* t_scale, int homogeneous, double clark_ell, float* Y, float* Pi,
@@ -563,11 +736,34 @@ extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, 
   }
   if (P == 0) return FIT_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  const long ntile = (P + 15) / 16;
-  long blocks = (ntile + 7) / 8;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  k_mlp_forward<<<(unsigned)blocks, 256, 0, st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi, homogeneous,
-                                                   (float)(clark_ell * clark_ell / 12.0));
+  const char* env = getenv("FIT_MLP_MMASYNC");   // the mma.sync forward (kept for comparison)
+  if (env && env[0] == '1') {
+    const long ntile = (P + 15) / 16;
+    long blocks = (ntile + 7) / 8;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_mlp_forward<<<(unsigned)blocks, 256, 0, st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi, homogeneous,
+                                                     (float)(clark_ell * clark_ell / 12.0));
+    FIT_LAUNCH_CHECK();
+    return FIT_OK;
+  }
+  static int* err = nullptr;   // wait-timeout flag of the tcgen05 forward (read by fit_mlp_status)
+  static int nsm = 0;
+  if (!err) {
+    FIT_CUDA_CHECK(cudaMalloc(&err, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(err, 0, sizeof(int)));
+    int dev = 0;
+    FIT_CUDA_CHECK(cudaGetDevice(&dev));
+    FIT_CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    FIT_CUDA_CHECK(cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(MlpTcSmem)));
+  }
+  g_mlp_err = err;
+  const long ntile = (P + 127) / 128;
+  long blocks = (long)nsm * 6;   // six CTAs per SM: 6 x 64 tensor-memory columns, ~6 x 34 KB shared memory
+  if (blocks > ntile) blocks = ntile;
+  k_mlp_forward_tc<<<(unsigned)blocks, 128, sizeof(MlpTcSmem), st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi,
+                                                                    homogeneous,
+                                                                    (float)(clark_ell * clark_ell / 12.0), err);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }

@@ -241,8 +241,12 @@ def _rel(a, b):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("homog,mixed", [(False, False), (True, False), (True, True)])
-def test_mlp_forward_matches_oracle(homog, mixed):
+def test_mlp_forward_matches_oracle(homog, mixed, kernel, monkeypatch):
+    """The forward on the fifth-generation tensor cores (default) and the warp-level mma.sync one."""
+    if kernel == "mma_sync":
+        monkeypatch.setenv("FIT_MLP_MMASYNC", "1")
     P, ld = 1000, 1037
     p, X, T, isc, tsc = _mlp_case(P, ld)
     m = F.SubfilterStressMLP(params=p, homogeneous=homog, mixed=mixed)
@@ -257,6 +261,31 @@ def test_mlp_forward_matches_oracle(homog, mixed):
     assert _rel(Y, Ye) <= 2e-3           # same BF16 rounding points, FP32 vs FP64 accumulation
     assert _rel(Y, Y64) <= 3e-2          # BF16 quantisation of weights, features and activations
     assert _rel(Pi, OC.flux_from_stress(Y.astype(np.float64), X[:, :P].astype(np.float64))) <= 1e-5
+    assert F._lib.mlp_status() == 0
+
+
+@pytest.mark.gpu
+def test_mlp_forward_tcgen05_tiles():
+    """tcgen05 forward on a point count that is not a multiple of its 128-point tile and on more
+    tiles than CTAs (grid-stride loop), against the mma.sync forward."""
+    import os
+    P, ld = 300_001, 300_007
+    rng = np.random.default_rng(4)
+    p = OC.mlp_init(9)
+    X = np.zeros((9, ld), np.float32)
+    X[:, :P] = rng.standard_normal((9, P))
+    m = F.SubfilterStressMLP(params=p, homogeneous=True, mixed=True)
+    m.ell = 0.5
+    Xd = _dev(X)
+    Y, Pi = m.predict(Xd, ld, P)
+    os.environ["FIT_MLP_MMASYNC"] = "1"
+    try:
+        Y2, Pi2 = m.predict(Xd, ld, P)
+    finally:
+        del os.environ["FIT_MLP_MMASYNC"]
+    assert F._lib.mlp_status() == 0
+    assert _rel(Y.cpu().numpy(), Y2.cpu().numpy()) <= 1e-4
+    assert _rel(Pi.cpu().numpy(), Pi2.cpu().numpy()) <= 1e-4
 
 
 @pytest.mark.gpu
