@@ -335,12 +335,23 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
     __syncthreads();
   };
   const long ntile = (P + 127) / 128;
+  float An[9];   // features of this thread's point in the next tile, loaded a tile ahead
+  {
+    const long p = (long)blockIdx.x * 128 + tid;
+#pragma unroll
+    for (int f = 0; f < 9; ++f) An[f] = p < P ? X[(long)f * ld + p] : 0.f;
+  }
   for (long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const long p = tile * 128 + tid;
     const bool live = p < P;
     float A[9], v[16];
 #pragma unroll
-    for (int f = 0; f < 9; ++f) A[f] = live ? X[(long)f * ld + p] : 0.f;
+    for (int f = 0; f < 9; ++f) A[f] = An[f];
+    {   // the loads of the next tile overlap this tile's MMA chain
+      const long pn = p + (long)gridDim.x * 128;
+#pragma unroll
+      for (int f = 0; f < 9; ++f) An[f] = pn < P ? X[(long)f * ld + pn] : 0.f;
+    }
     float q = 0.f;
 #pragma unroll
     for (int f = 0; f < 16; ++f) {
