@@ -245,6 +245,22 @@ def test_fused_shell_to_shell_64(deal, inv, herm, xpass, monkeypatch):
     assert rel(r.net_transfer, net) < 1e-4
 
 
+@pytest.mark.parametrize("n", [96, 128])
+@pytest.mark.parametrize("inv", ["ke", "helicity"])
+def test_fused_shell_to_shell_even_kx(n, inv):
+    """The fused pipeline on grids whose live box has an even number of x frequencies (96: KX = 32,
+    128: KX = 42; the x pass then pairs lines (c, c + C)) against the FP64 oracle."""
+    F.clear_plans()
+    u, ks = spectrum_field((n, n, n), e_config2, seed=11)
+    I = {"ke": F.KineticEnergy(), "helicity": F.Helicity()}[inv]
+    dk = n / 12.0
+    r = F.calculate_shell_to_shell_transfer(u, ks, binning=F.LinearBinning(dk), invariant=I,
+                                            spectral=F.GB300Spectral(32), execution=F.GB300Execution("batched"))
+    _, _, T, net, _ = O.shell_to_shell(u, ks, ("linear", dk), "two_thirds", inv)
+    assert rel(r.transfer_matrix, T) < 1e-5
+    assert rel(r.net_transfer, net) < 1e-4
+
+
 def test_fused_host_input_reads_only_kept_modes():
     """The fused 2/3 path copies only the kept slabs of a host field: values outside the kept box
     (NaN here) must not reach the result, which equals the clean field's and the oracle's."""
