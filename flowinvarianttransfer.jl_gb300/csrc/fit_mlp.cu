@@ -417,6 +417,316 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
   if (warp == 0) tmem_dealloc(tbase, 64);
 }
 
+// ---- training step on tcgen05 -------------------------------------------------------------------
+// One CTA of 128 threads per SM walks tiles of 128 points (one point per thread and tensor-memory
+// lane). Per tile, six MMA rounds: the three forward layers, dH2 = dY W3, dH1 = dZ2 W2 (M = 128,
+// point-major A tiles), then the weight gradients, which reduce over the points (K = 128) and
+// therefore read point-contiguous ("transposed") tiles written column-wise by the threads:
+//   G2: [dZ2T; dZ1T] x H1T -> rows 0..63 = dW2[h2][h1]
+//   G1: [dZ2T; dZ1T] x XT' -> rows 64..127 = dW1[h1][f] (f < 9) and db1 (f = 9: XT' row 9 is ones)
+//   G3: [H2T; dZ2T] x dYT' -> rows 0..63 = dW3[o][h2] transposed (o < 6), rows 64..127 col 8 = db2
+//        (dYT' row 8 is ones)
+// H2T, dZ2T and dZ1T are consecutive 64-row blocks of one tile, so both stacked A operands are
+// plain descriptors. The gradient accumulators stay in tensor memory across the CTA's tiles and
+// are added to grad once; db3 and the loss are reduced on the CUDA cores. ReLU masks of H1 and H2
+// are kept as 64-bit registers per point.
+struct MlpTrainTcSmem {
+  __nv_bfloat16 W1[64 * 16], W2[64 * 64], W3[16 * 64], W2T[64 * 64], W3T[64 * 16];   // canonical layouts
+  __nv_bfloat16 A1[128 * 16];    // layer-1 A tile, then dY (point-major, K = 16)
+  __nv_bfloat16 A2[128 * 64];    // H1, H2, then dZ2 (point-major)
+  __nv_bfloat16 XT[16 * 128];    // features (rows 0..8), ones (row 9), point-contiguous
+  __nv_bfloat16 H1T[64 * 128];
+  __nv_bfloat16 ST[192 * 128];   // H2T | dZ2T | dZ1T
+  __nv_bfloat16 dYT[16 * 128];   // dY (rows 0..5), ones (row 8)
+  float b1[64], b2[64], b3[8], sc[9], tsc[6], db3[8];
+  double lsum[4];
+  uint64_t bar;
+  uint32_t tmem;
+};
+
+FIT_D void st_col(__nv_bfloat16* tile, int row, int p, float v) {   // element (row, point p), K = 128
+  st_bf16_at(tile, umma_off(row, p, 128), v);
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_train_tc(const float* __restrict__ Pm, const float* __restrict__ X,
+                                                         const float* __restrict__ T, long ld, long P, long Ptot,
+                                                         const float* __restrict__ in_scale,
+                                                         const float* __restrict__ t_scale, float* __restrict__ grad,
+                                                         double* __restrict__ loss, int homog, int* err) {
+  extern __shared__ __align__(128) unsigned char mlp_tr_raw[];
+  MlpTrainTcSmem& S = *reinterpret_cast<MlpTrainTcSmem*>(mlp_tr_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < 64 * 16; i += 128) st_bf16_at(S.W1, umma_off(i / 16, i % 16, 16), Pm[MlpOff::W1 + i]);
+  for (int i = tid; i < 64 * 64; i += 128) {
+    const int r = i / 64, c = i % 64;
+    const float w = Pm[MlpOff::W2 + i];
+    st_bf16_at(S.W2, umma_off(r, c, 64), w);
+    st_bf16_at(S.W2T, umma_off(c, r, 64), w);
+  }
+  for (int i = tid; i < 16 * 64; i += 128) {   // W3 padded to 16 output rows; W3T[h][o], o padded to 16
+    const int r = i / 64, c = i % 64;
+    const float w = r < 8 ? Pm[MlpOff::W3 + i] : 0.f;
+    st_bf16_at(S.W3, umma_off(r, c, 64), w);
+    st_bf16_at(S.W3T, umma_off(c, r, 16), w);
+  }
+  for (int i = tid; i < 16 * 128; i += 128) {   // constant rows of XT' and dYT'
+    const int r = i / 128, p = i % 128;
+    st_col(S.XT, r, p, r == 9 ? 1.f : 0.f);
+    st_col(S.dYT, r, p, r == 8 ? 1.f : 0.f);
+  }
+  if (tid < 64) {
+    S.b1[tid] = Pm[MlpOff::B1 + tid];
+    S.b2[tid] = Pm[MlpOff::B2 + tid];
+  }
+  if (tid < 8) {
+    S.b3[tid] = Pm[MlpOff::B3 + tid];
+    S.db3[tid] = 0.f;
+  }
+  if (tid < 9) S.sc[tid] = in_scale[tid];
+  if (tid < 6) S.tsc[tid] = t_scale[tid];
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    mbar_init_fence();
+  }
+  if (warp == 0) {
+    tmem_alloc(&S.tmem, 256);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tmem;
+  const uint32_t tl = tbase + ((uint32_t)(warp * 32) << 16);
+  const uint32_t TD = tbase, TG2 = tbase + 64, TG1 = tbase + 128, TG3 = tbase + 144;   // column bases
+  const uint32_t aA1 = smem_u32(S.A1), aA2 = smem_u32(S.A2), aXT = smem_u32(S.XT), aH1T = smem_u32(S.H1T);
+  const uint32_t aST = smem_u32(S.ST), adYT = smem_u32(S.dYT);
+  const uint32_t aW1 = smem_u32(S.W1), aW2 = smem_u32(S.W2), aW3 = smem_u32(S.W3);
+  const uint32_t aW2T = smem_u32(S.W2T), aW3T = smem_u32(S.W3T);
+  constexpr uint32_t ID64 = umma_idesc_bf16(128, 64), ID16 = umma_idesc_bf16(128, 16);
+  __nv_bfloat16* H2T = S.ST;
+  __nv_bfloat16* dZ2T = S.ST + 64 * 128;
+  __nv_bfloat16* dZ1T = S.ST + 128 * 128;
+  uint32_t phase = 0;
+  bool failed = false;
+  auto wait_mma = [&]() {
+    if (!mbar_wait_bounded(&S.bar, phase, 2000000000LL)) failed = true;
+    phase ^= 1u;
+    tc_fence_after();
+  };
+  auto publish = [&]() {
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+  };
+  const float inv = 2.f / (float)Ptot;
+  double lsum = 0.0;
+  float db3[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  bool first = true;
+  const long ntile = (P + 127) / 128;
+  for (long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const long p = tile * 128 + tid;
+    const bool live = p < P;
+    // (a) features -> A1 row and XT column
+    float v[16];
+    float q = 0.f;
+#pragma unroll
+    for (int f = 0; f < 16; ++f) {
+      v[f] = (f < 9 && live) ? X[(long)f * ld + p] * S.sc[f] : 0.f;
+      q += v[f] * v[f];
+    }
+    const float sn = homog ? q : 1.f;
+    if (homog) {
+      const float iq = q > 0.f ? 1.f / sqrtf(q) : 0.f;
+#pragma unroll
+      for (int f = 0; f < 16; ++f) v[f] *= iq;
+    }
+    st_chunk(S.A1, umma_off(tid, 0, 16), v);
+    st_chunk(S.A1, umma_off(tid, 8, 16), v + 8);
+#pragma unroll
+    for (int f = 0; f < 9; ++f) st_col(S.XT, f, tid, v[f]);
+    publish();
+    if (tid == 0) {
+      tc_fence_after();
+      umma_bf16(TD, umma_desc(aA1, 128, 256), umma_desc(aW1, 128, 256), ID64, false);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    // (b) H1 = relu(D + b1): A2 row, H1T column, mask
+    uint32_t m1[2] = {0u, 0u}, m2[2] = {0u, 0u};
+#pragma unroll
+    for (int c4 = 0; c4 < 4; ++c4) {
+      float d[16];
+      tmem_ld16(tl + 16 * c4, d);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int h = 16 * c4 + i;
+        d[i] = fmaxf(d[i] + S.b1[h], 0.f);
+        if (d[i] > 0.f) m1[h >> 5] |= 1u << (h & 31);
+        st_col(S.H1T, h, tid, d[i]);
+      }
+      st_chunk(S.A2, umma_off(tid, 16 * c4, 64), d);
+      st_chunk(S.A2, umma_off(tid, 16 * c4 + 8, 64), d + 8);
+    }
+    publish();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        umma_bf16(TD, umma_desc(aA2 + 256 * k, 128, 1024), umma_desc(aW2 + 256 * k, 128, 1024), ID64, k > 0);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    // (c) H2 = relu(D + b2): A2 row (layer 2 has read H1), H2T column, mask
+#pragma unroll
+    for (int c4 = 0; c4 < 4; ++c4) {
+      float d[16];
+      tmem_ld16(tl + 16 * c4, d);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int h = 16 * c4 + i;
+        d[i] = fmaxf(d[i] + S.b2[h], 0.f);
+        if (d[i] > 0.f) m2[h >> 5] |= 1u << (h & 31);
+        st_col(H2T, h, tid, d[i]);
+      }
+      st_chunk(S.A2, umma_off(tid, 16 * c4, 64), d);
+      st_chunk(S.A2, umma_off(tid, 16 * c4 + 8, 64), d + 8);
+    }
+    publish();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        umma_bf16(TD, umma_desc(aA2 + 256 * k, 128, 1024), umma_desc(aW3 + 256 * k, 128, 1024), ID16, k > 0);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    // (d) loss and dY = 2 (s y - t T) s / Ptot: A1 row (point-major), dYT column
+    {
+      float y[16], dy[16];
+      tmem_ld16(tl, y);
+#pragma unroll
+      for (int o = 0; o < 16; ++o) {
+        float d = 0.f;
+        if (o < 6 && live) {
+          const float diff = (y[o] + S.b3[o]) * sn - T[(long)o * ld + p] * S.tsc[o];
+          lsum += (double)diff * diff;
+          d = inv * diff * sn;
+        }
+        dy[o] = __bfloat162float(__float2bfloat16_rn(d));   // the value the MMAs see
+      }
+#pragma unroll
+      for (int o = 0; o < 6; ++o) {
+        db3[o] += dy[o];
+        st_col(S.dYT, o, tid, dy[o]);
+      }
+      st_chunk(S.A1, umma_off(tid, 0, 16), dy);
+      st_chunk(S.A1, umma_off(tid, 8, 16), dy + 8);
+    }
+    publish();
+    if (tid == 0) {
+      tc_fence_after();
+      umma_bf16(TD, umma_desc(aA1, 128, 256), umma_desc(aW3T, 128, 256), ID64, false);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    // (e) dZ2 = dH2 * (H2 > 0): A2 row (layer 3 has read H2), dZ2T column
+#pragma unroll
+    for (int c4 = 0; c4 < 4; ++c4) {
+      float d[16];
+      tmem_ld16(tl + 16 * c4, d);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int h = 16 * c4 + i;
+        d[i] = (m2[h >> 5] >> (h & 31)) & 1u ? d[i] : 0.f;
+        st_col(dZ2T, h, tid, d[i]);
+      }
+      st_chunk(S.A2, umma_off(tid, 16 * c4, 64), d);
+      st_chunk(S.A2, umma_off(tid, 16 * c4 + 8, 64), d + 8);
+    }
+    publish();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        umma_bf16(TD, umma_desc(aA2 + 256 * k, 128, 1024), umma_desc(aW2T + 256 * k, 128, 1024), ID64, k > 0);
+      umma_commit(&S.bar);
+    }
+    wait_mma();
+    // (f) dZ1 = dH1 * (H1 > 0): dZ1T column
+#pragma unroll
+    for (int c4 = 0; c4 < 4; ++c4) {
+      float d[16];
+      tmem_ld16(tl + 16 * c4, d);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int h = 16 * c4 + i;
+        st_col(dZ1T, h, tid, (m1[h >> 5] >> (h & 31)) & 1u ? d[i] : 0.f);
+      }
+    }
+    publish();
+    // (g) weight gradients, accumulated over the CTA's tiles in tensor memory
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t aS2 = aST + 8 * 2048;   // dZ2T: the stack [dZ2T; dZ1T]
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const bool acc = !first || k > 0;
+        umma_bf16(TG2, umma_desc(aS2 + 256 * k, 128, 2048), umma_desc(aH1T + 256 * k, 128, 2048), ID64, acc);
+        umma_bf16(TG1, umma_desc(aS2 + 256 * k, 128, 2048), umma_desc(aXT + 256 * k, 128, 2048), ID16, acc);
+        umma_bf16(TG3, umma_desc(aST + 256 * k, 128, 2048), umma_desc(adYT + 256 * k, 128, 2048), ID16, acc);
+      }
+      umma_commit(&S.bar);
+    }
+    wait_mma();   // the tiles read by the gradient MMAs are rewritten by the next tile
+    first = false;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  // flush: loss and db3 on the CUDA cores, the tensor-memory gradients by their owning threads
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+#pragma unroll
+  for (int o = 0; o < 6; ++o) {
+    float sdb = db3[o];
+    for (int k = 16; k > 0; k >>= 1) sdb += __shfl_down_sync(0xffffffffu, sdb, k);
+    if (lane == 0) atomicAdd(&S.db3[o], sdb);
+  }
+  if (lane == 0) S.lsum[warp] = lsum;
+  if (!first) {   // this CTA processed at least one tile
+    if (warp < 2) {   // lanes 0..63: dW2 rows h2, dW3^T rows h2
+      const int h2 = tid;
+#pragma unroll
+      for (int c4 = 0; c4 < 4; ++c4) {
+        float d[16];
+        tmem_ld16(tl + 64 + 16 * c4, d);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) atomicAdd(&grad[MlpOff::W2 + h2 * 64 + 16 * c4 + i], d[i]);
+      }
+      float d[16];
+      tmem_ld16(tl + 144, d);
+#pragma unroll
+      for (int o = 0; o < 6; ++o) atomicAdd(&grad[MlpOff::W3 + o * 64 + h2], d[o]);
+    } else {   // lanes 64..127: dW1 rows h1 with db1, db2
+      const int h = tid - 64;
+      float d[16];
+      tmem_ld16(tl + 128, d);
+#pragma unroll
+      for (int f = 0; f < 9; ++f) atomicAdd(&grad[MlpOff::W1 + h * 16 + f], d[f]);
+      atomicAdd(&grad[MlpOff::B1 + h], d[9]);
+      tmem_ld16(tl + 144, d);
+      atomicAdd(&grad[MlpOff::B2 + h], d[8]);
+    }
+  }
+  if (failed) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid < 6) atomicAdd(&grad[MlpOff::B3 + tid], S.db3[tid]);
+  if (tid == 0) atomicAdd(loss, S.lsum[0] + S.lsum[1] + S.lsum[2] + S.lsum[3]);
+  if (warp == 0) tmem_dealloc(tbase, 256);
+}
+
 // ---- training: fused forward + backward, weight gradients reduced over points by MMAs --------------
 // A block of 4 warps handles 64 points per iteration (16 per warp). Activations are staged in shared
 // memory transposed (feature-major, 64 points contiguous) so that the weight-gradient products
@@ -720,7 +1030,16 @@ __global__ void k_compare(const float* __restrict__ a, const float* __restrict__
 
 using namespace fit;
 
-static int* g_mlp_err = nullptr;
+static int* g_mlp_err = nullptr;   // wait-timeout flag of the tcgen05 kernels (read by fit_mlp_status)
+
+static int mlp_err_flag(int** out) {
+  if (!g_mlp_err) {
+    FIT_CUDA_CHECK(cudaMalloc(&g_mlp_err, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(g_mlp_err, 0, sizeof(int)));
+  }
+  *out = g_mlp_err;
+  return FIT_OK;
+}
 
 extern "C" int fit_mlp_nparams(void) { return MLP_NPARAM; }
 
@@ -757,18 +1076,16 @@ extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, 
     FIT_LAUNCH_CHECK();
     return FIT_OK;
   }
-  static int* err = nullptr;   // wait-timeout flag of the tcgen05 forward (read by fit_mlp_status)
+  int* err = nullptr;
+  FIT_TRY(mlp_err_flag(&err));
   static int nsm = 0;
-  if (!err) {
-    FIT_CUDA_CHECK(cudaMalloc(&err, sizeof(int)));
-    FIT_CUDA_CHECK(cudaMemset(err, 0, sizeof(int)));
+  if (!nsm) {
     int dev = 0;
     FIT_CUDA_CHECK(cudaGetDevice(&dev));
     FIT_CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     FIT_CUDA_CHECK(cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sizeof(MlpTcSmem)));
   }
-  g_mlp_err = err;
   const long ntile = (P + 127) / 128;
   long blocks = (long)nsm * 6;   // six CTAs per SM: 6 x 64 tensor-memory columns, ~6 x 34 KB shared memory
   if (blocks > ntile) blocks = ntile;
@@ -787,6 +1104,26 @@ extern "C" int fit_mlp_train_grad(const float* params, const float* X, const flo
     return FIT_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
+  const char* env = getenv("FIT_MLP_MMASYNC");   // the mma.sync training step (kept for comparison)
+  if (!(env && env[0] == '1')) {
+    int* err = nullptr;
+    FIT_TRY(mlp_err_flag(&err));
+    static bool tc_attr = false;
+    if (!tc_attr) {
+      FIT_CUDA_CHECK(cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)sizeof(MlpTrainTcSmem)));
+      tc_attr = true;
+    }
+    int dev = 0, nsm = 0;
+    FIT_CUDA_CHECK(cudaGetDevice(&dev));
+    FIT_CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const long ntile = (P + 127) / 128;
+    const long blocks = ntile < nsm ? ntile : nsm;   // one CTA per SM (256 tensor-memory columns, ~117 KB)
+    k_mlp_train_tc<<<(unsigned)blocks, 128, sizeof(MlpTrainTcSmem), st>>>(params, X, T, ld, P, Ptot, in_scale,
+                                                                           t_scale, grad, loss, homogeneous, err);
+    FIT_LAUNCH_CHECK();
+    return FIT_OK;
+  }
   const long nblk = (P + 63) / 64;
   long blocks = nblk < 152 * 4 ? nblk : 152 * 4;
   const size_t smem = ((sizeof(MlpSmem) + 15) / 16) * 16 + sizeof(MlpTrainSmem);

@@ -289,8 +289,12 @@ def test_mlp_forward_tcgen05_tiles():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("homog", [False, True])
-def test_mlp_gradient_matches_oracle(homog):
+def test_mlp_gradient_matches_oracle(homog, kernel, monkeypatch):
+    """The training step on the fifth-generation tensor cores (default) and the mma.sync one."""
+    if kernel == "mma_sync":
+        monkeypatch.setenv("FIT_MLP_MMASYNC", "1")
     P, ld = 1000, 1037
     p, X, T, isc, tsc = _mlp_case(P, ld, seed=5)
     m = F.SubfilterStressMLP(params=p, homogeneous=homog)
@@ -306,6 +310,7 @@ def test_mlp_gradient_matches_oracle(homog):
         assert _rel(gd[k], ged[k]) <= 5e-3, k
         assert _rel(gd[k], g64d[k]) <= 5e-2, k
     assert np.all(gd["W1"][:, 9:] == 0) and np.all(gd["W3"][6:] == 0)
+    assert F._lib.mlp_status() == 0
 
 
 @pytest.mark.gpu
