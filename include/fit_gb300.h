@@ -208,9 +208,9 @@ int fit_autotune_entry(int64_t i, int64_t* fields, double* ms);
 /* ---- learned subfilter-stress closure (no counterpart in the reference) -------------------------
  * A pointwise MLP 9 -> 64 -> 64 -> 6 (ReLU) maps the filtered velocity-gradient tensor A_ij = d_j ū_i
  * (9 features) to the six subfilter-stress components (tau_00 tau_11 tau_22 tau_01 tau_02 tau_12).
- * Tensor-core kernels: BF16 operands (weights, features, activations), FP32 accumulation; the forward
- * runs on the fifth-generation tensor cores (tcgen05 MMAs, accumulators in tensor memory), the
- * training step on warp-level mma.sync. params is
+ * Tensor-core kernels: BF16 operands (weights, features, activations), FP32 accumulation, on the
+ * fifth-generation tensor cores (tcgen05 MMAs, accumulators in tensor memory) for both the forward
+ * and the training step. params is
  * the FP32 master copy (fit_mlp_nparams() floats: W1[64][16], b1[64], W2[64][64], b2[64], W3[8][64],
  * b3[8]; input columns 9..15 and output rows 6..7 are padding that stays zero). Point data is
  * field-major with field stride ld >= P: X[9][ld], T/Y[6][ld]. Features are multiplied by
@@ -224,8 +224,8 @@ int fit_mlp_nparams(void);
  * network is a residual over the gradient model and ell^2/12 A A^T is added to its output. */
 int fit_mlp_forward(const float* params, const float* X, int64_t ld, int64_t P, const float* in_scale,
                     const float* t_scale, int homogeneous, double clark_ell, float* Y, float* Pi, void* stream);
-/* *timed_out = 1 when a clock-bounded wait of an earlier fit_mlp_forward gave up (its outputs are then
- * not valid); reading synchronises the device and clears the flag. */
+/* *timed_out = 1 when a clock-bounded wait of an earlier fit_mlp_forward or fit_mlp_train_grad gave
+ * up (its outputs are then not valid); reading synchronises the device and clears the flag. */
 int fit_mlp_status(int* timed_out);
 /* out (6 x ld) = tau - ell^2/12 A A^T: residual targets of a network trained over the gradient model. */
 int fit_stress_residual(const float* A, const float* tau, int64_t ld, int64_t P, double ell, float* out,
