@@ -39,4 +39,16 @@ int fz_velocity_a(int N, const FzArgs& a, const float2* H, float2* bufZ, float2*
   }
 }
 
+// Whole-box nonlinear terms of a batch (1 when N is not built here).
+int fz_terms_a(int N, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA, float2* bufB,
+               float2* Nout, const float2* tw, int* err, cudaStream_t st) {
+  switch (N) {
+    case 64: return fz_terms<64>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    case 128: return fz_terms<128>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    case 256: return fz_terms<256>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    case 512: return fz_terms<512>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    default: return 1;
+  }
+}
+
 }  // namespace fit

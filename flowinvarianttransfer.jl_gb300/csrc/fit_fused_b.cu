@@ -39,4 +39,16 @@ int fz_velocity_b(int N, const FzArgs& a, const float2* H, float2* bufZ, float2*
   }
 }
 
+// Whole-box nonlinear terms of a batch (1 when N is not built here).
+int fz_terms_b(int N, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA, float2* bufB,
+               float2* Nout, const float2* tw, int* err, cudaStream_t st) {
+  switch (N) {
+    case 96: return fz_terms<96>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    case 192: return fz_terms<192>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    case 384: return fz_terms<384>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    case 768: return fz_terms<768>(a, H, kd, U, bufA, bufB, Nout, tw, err, st);
+    default: return 1;
+  }
+}
+
 }  // namespace fit

@@ -49,6 +49,10 @@ struct FzArgs {
   const unsigned* zoff;
   const uint16_t* zent;
   int ntile;
+  // batches of whole-box terms (partial fluxes): mediator b advects field hidx[b] of the H array
+  // (3 KY P1 complex values each) by velocity uidx[b] of the U array (3 N^3 floats each)
+  int hidx[16];
+  int uidx[16];
 };
 
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
@@ -189,6 +193,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const flo
   const int b = blockIdx.x;
   const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
   const long Mtot = (long)N * N * N;
+  U += (long)a.uidx[b] * 3 * Mtot;   // this mediator's advecting velocity
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   for (int c = 0; c < 3; ++c) {
     float2 acc[EPT];
@@ -287,6 +292,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
   const int b = blockIdx.x;
   const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
   const long Mtot = (long)N * N * N;
+  U += (long)a.uidx[b] * 3 * Mtot;   // this mediator's advecting velocity
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -435,6 +441,7 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
   const int b = blockIdx.x;
   const int ex = a.ext[b][0];   // gradient inputs are zero beyond the mediator's x extent
   const long Mtot = (long)N * N * N;
+  U += (long)a.uidx[b] * 3 * Mtot;   // this mediator's advecting velocity
   // the two lines of complex column c: gradient rows ra, rb of the (line-ordered) staging tile;
   // velocity line r lands in row urow(r), so that column c reads velocity rows c and c + C
   // (4-bank row offsets with rows of N + 4 floats: conflict-free for a warp's 8 columns)
@@ -644,6 +651,74 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
   for (int t = tid; t < a.nsh; t += NT) pb[(long)t * gridDim.z] = bins[t];
 }
 
+// ---- whole-box terms (partial fluxes) -------------------------------------------------------------
+// z pass of a whole live box (no shell restriction): mediator b transforms field hidx[b] of H and
+// its ik_z derivative; outputs as zinv's.
+template <int N>
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_box(FzArgs a, const float2* __restrict__ H,
+                                                                              const float* __restrict__ kd,
+                                                                              float2* __restrict__ out,
+                                                                              const float2* __restrict__ twg) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const long c0 = (long)blockIdx.z * C;
+  const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  const float2* Hc = H + ((long)a.hidx[b] * 3 + c) * a.KY * a.P1;
+  float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1;
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const long col = c0 + cc;
+        const int f = fz_freq(e, N);
+        float2 val = make_float2(0.f, 0.f);
+        if (col < a.P1 && f >= -a.K && f <= a.K) {
+          val = Hc[(long)(f + a.K) * a.P1 + col];
+          if (v) val = fz_muli(val, kd[f + a.K]);
+        }
+        return val;
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const long col = c0 + cc;
+        if (col < a.P1) ob[(long)e * a.P1 + col] = val;
+      });
+}
+
+// forward z pass of yfwd's output, kept in the live box: out [b][c][kz'][col] (the nonlinear term)
+template <int N>
+__global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zfwd_store(FzArgs a, const float2* __restrict__ in,
+                                                                                float2* __restrict__ out,
+                                                                                const float2* __restrict__ twg) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw);
+  float2* tw = s + E;
+  const int tid = threadIdx.x;
+  const long c0 = (long)blockIdx.z * C;
+  const int c = blockIdx.y, b = blockIdx.x;
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
+  __syncthreads();
+  const float2* ib = in + ((long)b * 3 + c) * N * a.P1;
+  float2* ob = out + ((long)b * 3 + c) * a.KY * a.P1;
+  ct_fft_mapped<float2, false, N, C, NT, TT::EPT>(
+      s, tw, tid,
+      [&](int, int, int e, int cc) -> float2 {
+        const long col = c0 + cc;
+        return (col < a.P1) ? ib[(long)e * a.P1 + col] : make_float2(0.f, 0.f);
+      },
+      [&](int, int, int e, int cc, float2 val) {
+        const long col = c0 + cc;
+        const int f = fz_freq(e, N);
+        if (col < a.P1 && f >= -a.K && f <= a.K) ob[(long)(f + a.K) * a.P1 + col] = val;
+      });
+}
+
 // ---- self-advecting velocity in physical space from H ------------------------------------------
 // U = real(ifft3(Herm part of the masked velocity)) over the live box only: z pass of the KX x KY
 // live pencils, y pass of the live kx columns, x pass two Hermitian lines per complex transform.
@@ -814,6 +889,79 @@ int fz_velocity(const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, fl
   return FIT_OK;
 }
 
+// ---- the x pass of a batch: register-accumulating form where its tiles fit, else staged ---------
+template <int N>
+int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, const float2* tw, int* err,
+             cudaStream_t st) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C;
+  typedef XTile<N> XT;
+  const size_t smx = XT::SMEM_FIXED + 2 * (size_t)(2 * XT::C * a.KX) * 8;
+  const bool bulk = smx <= 227 * 1024 && (a.L % (2 * XT::C)) == 0;   // 16-byte alignment holds: L, 2C are multiples of 16
+  typedef XRTile<N> XR;
+  const size_t smr = XR::OFF_G + 2 * (size_t)(2 * XR::C * a.KX) * 8;
+  const char* env = getenv("FIT_XMIX_BULK");   // selects the previous form of the x pass
+  bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
+  if constexpr (XR::OK) {
+    if (reg) {
+      FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
+      FzArgs ax = a;
+      ax.xpair = fz_xpair(a.KX, XR::C);
+      k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, G, U, out, tw, err);
+    }
+  }
+  if (reg) {
+  } else if (bulk) {
+    FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx, XT::NTHR));
+    k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, G, U, out, tw, err);
+  } else {
+    FIT_TRY(ct_prep_fused(k_fz_xmix<N>, TT::SMEM, TT::NTHR));
+    k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, TT::SMEM, st>>>(a, G, U, out,
+                                                                                                     tw);
+  }
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+// ---- host launcher for a batch of whole-box nonlinear terms (instantiated per transform length) ---
+// Mediator b: N_b = (u_{uidx[b]} . grad) f_{hidx[b]} over the whole live box (a.ext all K), written
+// to Nout [b][c][kz'][col]. Scratch as fz_batch.
+template <int N>
+int fz_terms(const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA, float2* bufB,
+             float2* Nout, const float2* tw, int* err, cudaStream_t st) {
+  typedef FzTile<N> TT;
+  constexpr int C = TT::C;
+  const size_t sm = TT::SMEM;
+  FIT_TRY(ct_prep_fused(k_fz_zinv_box<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_yinv<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_xmix<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_yfwd<N>, sm, TT::NTHR));
+  FIT_TRY(ct_prep_fused(k_fz_zfwd_store<N>, sm, TT::NTHR));
+  const unsigned pt = (unsigned)((a.P1 + C - 1) / C);
+  const unsigned nkt = (unsigned)((a.KX + C - 1) / C);
+  const double cpx = 8.0, L = (double)N * N;
+  fit_prof_begin(PK_S2S_ZINV, cpx * a.nb * (3.0 * a.KY * a.P1 + 6.0 * N * a.P1), st);
+  k_fz_zinv_box<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, kd, bufA, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_YINV, cpx * a.nb * (6.0 * N * a.P1 + 9.0 * L * a.KX), st);
+  k_fz_yinv<N><<<dim3(a.nb, 9, nkt * N), TT::NTHR, sm, st>>>(a, bufA, kd, bufB, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_XMIX, cpx * a.nb * (9.0 * L * a.KX + 3.0 * L * a.KX) + 4.0 * 3.0 * N * L * 2, st);
+  FIT_TRY(fz_xpass<N>(a, bufB, U, bufA, tw, err, st));
+  fit_prof_end(st);
+  fit_prof_begin(PK_S2S_YFWD, cpx * a.nb * (3.0 * L * a.KX + 3.0 * N * a.P1), st);
+  k_fz_yfwd<N><<<dim3(a.nb, 3, nkt * N), TT::NTHR, sm, st>>>(a, bufA, bufB, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  fit_prof_begin(PK_S2S_ZFWD_BIN, cpx * a.nb * (3.0 * N * a.P1 + 3.0 * a.KY * a.P1), st);
+  k_fz_zfwd_store<N><<<dim3(a.nb, 3, pt), TT::NTHR, sm, st>>>(a, bufB, Nout, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 // ---- host launcher for one batch (instantiated per transform length) -------------------------
 template <int N>
 int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
@@ -852,35 +1000,8 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_XMIX,
                  cpx * a.nb * (9.0 * (double)N * N * a.KX + 3.0 * (double)N * N * a.KX) + 4.0 * 3.0 * N * N * N, st);
-  {
-    typedef XTile<N> XT;
-    const size_t smx = XT::SMEM_FIXED + 2 * (size_t)(2 * XT::C * a.KX) * 8;
-    const bool bulk = smx <= 227 * 1024 && (a.L % (2 * XT::C)) == 0;   // 16-byte alignment holds: L, 2C are multiples of 16
-    typedef XRTile<N> XR;
-    const size_t smr = XR::OFF_G + 2 * (size_t)(2 * XR::C * a.KX) * 8;
-    const char* env = getenv("FIT_XMIX_BULK");   // selects the previous form of the x pass
-    bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
-    if constexpr (XR::OK) {
-      if (reg) {
-        FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
-        FzArgs ax = a;
-        ax.xpair = fz_xpair(a.KX, XR::C);
-        k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, bufB, U, bufA,
-                                                                                              tw, err);
-      }
-    }
-    if (reg) {
-    } else if (bulk) {
-      FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx, XT::NTHR));
-      k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, bufB, U, bufA, tw,
-                                                                                             err);
-    } else {
-      k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, sm, st>>>(a, bufB, U, bufA,
-                                                                                                tw);
-    }
-  }
+  FIT_TRY(fz_xpass<N>(a, bufB, U, bufA, tw, err, st));
   fit_prof_end(st);
-  FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_YFWD, cpx * a.nb * (3.0 * (double)N * N * a.KX + 3.0 * N * a.P1), st);
   k_fz_yfwd<N><<<dim3(a.nb, 3, nkt * N), TT::NTHR, sm, st>>>(a, bufA, bufB, tw);
   fit_prof_end(st);

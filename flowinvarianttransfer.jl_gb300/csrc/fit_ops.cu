@@ -293,8 +293,10 @@ __global__ void k_reduce_partials(const double* __restrict__ partial, int nblock
 template <typename T>
 int bin_density_multi(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,
                       const typename Vec2<T>::t* ceff, long ceff_set_stride, int nset, int nc, const uint16_t* seff,
-                      int nsh, double* partial, long partial_cap, const BinOut& out, cudaStream_t st) {
+                      int nsh, double* partial, long partial_cap, const BinOut& out, cudaStream_t st,
+                      long len) {
   typedef typename Vec2<T>::t V;
+  const long L = len < 0 ? g.Mhalf : len;
   if (nset < 1 || nset > 8) {
     fit_set_error("binning: 1..8 carrier sets per pass (got %d)", nset);
     return FIT_ERR_ARG;
@@ -306,7 +308,7 @@ int bin_density_multi(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_
     return FIT_ERR_SIZE;
   }
   int nblocks = 2 * 152;
-  const long needed = (g.Mhalf + 255) / 256;
+  const long needed = (L + 255) / 256;
   if (needed < nblocks) nblocks = (int)needed;
   if ((long)nblocks * nbins > partial_cap) nblocks = (int)(partial_cap / nbins);
   if (nblocks < 1) {
@@ -322,13 +324,13 @@ int bin_density_multi(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_
       return FIT_ERR_CUDA;
     }
   }
-  fit_prof_begin(PK_BIN, (double)g.Mhalf * ((nb + nset) * nc * sizeof(V) + 2.0), st);
+  fit_prof_begin(PK_BIN, (double)L * ((nb + nset) * nc * sizeof(V) + 2.0), st);
   if (f32)
-    k_bin<V, float><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, ceff_set_stride, nset, nc, seff, g.Mhalf,
+    k_bin<V, float><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, ceff_set_stride, nset, nc, seff, L,
                                                nsh, partial);
   else
     k_bin<V, double><<<nblocks, 256, smem, st>>>(nh, nh_batch_stride, nb, ceff, ceff_set_stride, nset, nc, seff,
-                                                g.Mhalf, nsh, partial);
+                                                L, nsh, partial);
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   k_reduce_partials<<<nblk(nbins, 128), 128, 0, st>>>(partial, nblocks, nbins, nb * nsh, out);
@@ -616,9 +618,9 @@ template int effective_carrier<float>(const GridDesc&, const KTab&, const void*,
 template int effective_carrier<double>(const GridDesc&, const KTab&, const void*, int, long, int, int, int,
                                        const uint16_t*, double2*, int, uint16_t*, cudaStream_t);
 template int bin_density_multi<float>(const GridDesc&, const float2*, long, int, const float2*, long, int, int,
-                                      const uint16_t*, int, double*, long, const BinOut&, cudaStream_t);
+                                      const uint16_t*, int, double*, long, const BinOut&, cudaStream_t, long);
 template int bin_density_multi<double>(const GridDesc&, const double2*, long, int, const double2*, long, int, int,
-                                       const uint16_t*, int, double*, long, const BinOut&, cudaStream_t);
+                                       const uint16_t*, int, double*, long, const BinOut&, cudaStream_t, long);
 template int bin_density<float>(const GridDesc&, const float2*, long, int, const float2*, int, const uint16_t*, int,
                                 double*, long, double*, cudaStream_t);
 template int bin_density<double>(const GridDesc&, const double2*, long, int, const double2*, int, const uint16_t*,

@@ -124,7 +124,8 @@ struct BinOut {
 template <typename T>
 int bin_density_multi(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_stride, int nb,
                       const typename Vec2<T>::t* ceff, long ceff_set_stride, int nset, int nc, const uint16_t* seff,
-                      int nsh, double* partial, long partial_cap, const BinOut& out, cudaStream_t st);
+                      int nsh, double* partial, long partial_cap, const BinOut& out, cudaStream_t st,
+                      long len = -1);   // modes per field (default: the half spectrum, g.Mhalf)
 
 // Shell sums: out[b*nsh + n] = sum_{g: seff(g)=n+1} sum_c Re(conj(ceff_c(g)) * nh_b,c(g)).
 template <typename T>

@@ -14,13 +14,27 @@
 
 #include <vector>
 
+#include "fit_fused_impl.cuh"
 #include "fit_gb300.h"
 #include "fit_plan.cuh"
 
 namespace fit {
 
+// live-box pipeline pieces (fit_s2s.cu)
+bool fz_box_ok(const fit_plan* p);
+void fz_box_dims(const fit_plan* p, FzArgs* a);
+int fz_box_setup(fit_plan* p, const FzArgs& a, const void* F, int inv, float2* H, float2* Ceff, uint16_t* seff,
+                 uint16_t* sb);
+int fz_box_kd(fit_plan* p, const FzArgs& a, float* kd);
+int fz_box_velocity(fit_plan* p, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U);
+int fz_box_terms(fit_plan* p, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA,
+                 float2* bufB, float2* Nout, int* err);
+
 struct PartialState {
   fit_dbuf comp, ceff, phys, hs, nph, nh;
+  // live-box form: H and carriers per component, velocities, scratch, the four terms, wait flag
+  fit_dbuf bH, bC, bse, bsb, bkd, bU, bA, bB, bN, berr;
+  int bkd_n = -1;
   cudaGraphExec_t exec = nullptr;
   long graph_launches = 0;
   // graph key
@@ -108,7 +122,91 @@ static int run_partial(fit_plan* p, PartialState* s, const void* ud, int decompo
   return FIT_OK;
 }
 
+// Live-box form for FP32 cubic 3D plans with a fused transform size: each component s gets H_s and
+// its carriers on the live box (k_fz_setup) and its velocity in physical space; the four terms
+// N = (u_sp . grad) u_sq run as one batch of four whole-box "mediators" through the fused passes
+// (z pass of H_sq, y pass, x pass with u_sp, forward y and z), and one binning pass takes all four
+// against every (invariant, s_k) carrier set.
+static int run_partial_box(fit_plan* p, PartialState* s, const void* ud, int decomposition, const int* invs,
+                           int ninv, double* Td) {
+  const GridDesc& g = p->g;
+  const size_t cb = (p->io_f64 ? 16 : 8) * (size_t)g.Ntot * 3;
+  FIT_TRY(pbuf(p, &s->comp, 2 * cb));
+  void* comp[2] = {s->comp.p, (char*)s->comp.p + cb};
+  if (decomposition == FIT_DECOMP_HELICAL) FIT_TRY(helical_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
+  else FIT_TRY(helmholtz_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
+  FzArgs a;
+  fz_box_dims(p, &a);
+  const long BL = (long)a.KY * a.P1;   // live-box modes per field
+  const double M = g.M[0];
+  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
+  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  FIT_TRY(pbuf(p, &s->bH, sizeof(float2) * 6 * BL));
+  FIT_TRY(pbuf(p, &s->bC, sizeof(float2) * 3 * BL * 2 * ninv));
+  FIT_TRY(pbuf(p, &s->bse, sizeof(uint16_t) * BL));
+  FIT_TRY(pbuf(p, &s->bsb, sizeof(uint16_t) * BL));
+  FIT_TRY(pbuf(p, &s->bkd, sizeof(float) * a.KY));
+  FIT_TRY(pbuf(p, &s->bU, sizeof(float) * 6 * g.Mtot));
+  FIT_TRY(pbuf(p, &s->bA, (size_t)(8.0 * perA * 4)));
+  FIT_TRY(pbuf(p, &s->bB, (size_t)(8.0 * perB * 4)));
+  FIT_TRY(pbuf(p, &s->bN, sizeof(float2) * 12 * BL));
+  if (!s->berr.p) {   // wait-timeout flag of the bulk-copy x pass (cleared once, outside capture)
+    FIT_TRY(pbuf(p, &s->berr, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(s->berr.p, 0, sizeof(int)));
+  }
+  if (s->bkd_n != a.KY) {   // never during a capture: the first call for a key runs eagerly
+    FIT_TRY(fz_box_kd(p, a, (float*)s->bkd.p));
+    s->bkd_n = a.KY;
+  }
+  float2* H = (float2*)s->bH.p;
+  float2* Cf = (float2*)s->bC.p;
+  for (int sk = 0; sk < 2; ++sk)
+    for (int j = 0; j < ninv; ++j)
+      FIT_TRY(fz_box_setup(p, a, comp[sk], invs[j], H + (long)sk * 3 * BL, Cf + (long)(j * 2 + sk) * 3 * BL,
+                           (uint16_t*)s->bse.p, (uint16_t*)s->bsb.p));
+  float* U = (float*)s->bU.p;
+  for (int sp = 0; sp < 2; ++sp)
+    FIT_TRY(fz_box_velocity(p, a, H + (long)sp * 3 * BL, (float2*)s->bA.p, (float2*)s->bB.p,
+                            U + (long)sp * 3 * g.Mtot));
+  a.nb = 4;
+  for (int b = 0; b < 4; ++b) {   // term b = (sp, sq): N = (u_sp . grad) u_sq  (src/SpectralFlux.jl:275)
+    a.uidx[b] = b >> 1;
+    a.hidx[b] = b & 1;
+    a.ext[b][0] = a.ext[b][1] = a.ext[b][2] = (short)a.K;
+  }
+  float2* Nb = (float2*)s->bN.p;
+  FIT_TRY(fz_box_terms(p, a, H, (const float*)s->bkd.p, U, (float2*)s->bA.p, (float2*)s->bB.p, Nb,
+                       (int*)s->berr.p));
+  // all four terms against every (invariant, s_k) carrier set in one binning pass:
+  // out.p[set][b * nsh + n] with set = j * 2 + sk lands at channel j * 8 + sk * 4 + b
+  const int nsh = p->nsh;
+  BinOut o;
+  for (int j = 0; j < ninv; ++j)
+    for (int sk = 0; sk < 2; ++sk) o.p[j * 2 + sk] = Td + ((size_t)j * 8 + sk * 4) * nsh;
+  const long cap = 2L * 152 * 2 * ninv * 4 * nsh;
+  FIT_TRY(ensure(p, &p->partial, sizeof(double) * cap));
+  FIT_TRY(bin_density_multi<float>(g, Nb, 3 * BL, 4, Cf, 3 * BL, 2 * ninv, 3, (const uint16_t*)s->bse.p, nsh,
+                                   (double*)p->partial.p, cap, o, p->stream, BL));
+  return FIT_OK;
+}
+
+// A bounded wait inside the live-box x pass that gave up leaves its flag set: report it.
+static int partial_box_check(fit_plan* p) {
+  PartialState* s = (PartialState*)p->partial_state;
+  if (!s || !s->berr.p) return FIT_OK;
+  int h = 0;
+  FIT_CUDA_CHECK(cudaMemcpyAsync(&h, s->berr.p, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));
+  if (h) {
+    FIT_CUDA_CHECK(cudaMemset(s->berr.p, 0, sizeof(int)));
+    fit_set_error("a bulk-copy wait timed out inside the fused partial-flux kernels");
+    return FIT_ERR_STATE;
+  }
+  return FIT_OK;
+}
+
 static int run_any(fit_plan* p, PartialState* s, const void* ud, int dec, const int* invs, int ninv, double* Td) {
+  if (fz_box_ok(p) && p->nd == 3 && ninv <= 4) return run_partial_box(p, s, ud, dec, invs, ninv, Td);
   return p->prec == 64 ? run_partial<double>(p, s, ud, dec, invs, ninv, Td)
                        : run_partial<float>(p, s, ud, dec, invs, ninv, Td);
 }
@@ -182,7 +280,8 @@ void partial_free(fit_plan* p) {
   PartialState* s = (PartialState*)p->partial_state;
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
-  fit_dbuf* bufs[] = {&s->comp, &s->ceff, &s->phys, &s->hs, &s->nph, &s->nh};
+  fit_dbuf* bufs[] = {&s->comp, &s->ceff, &s->phys, &s->hs, &s->nph, &s->nh, &s->bH, &s->bC,
+                      &s->bse,  &s->bsb,  &s->bkd,  &s->bU, &s->bA,  &s->bB,  &s->bN, &s->berr};
   for (fit_dbuf* b : bufs) {
     if (b->p) {
       cudaFree(b->p);
@@ -252,6 +351,7 @@ extern "C" int fit_partial_fluxes_batched(fit_plan* p, const void* u_hat, int de
     Td = (double*)p->outd.p;
   }
   FIT_TRY(partial_batched(p, ud, decomposition, invariants, n_invariants, Td));
+  FIT_TRY(partial_box_check(p));
   if (ptr_kind != FIT_PTR_DEVICE) {
     FIT_CUDA_CHECK(cudaMemcpyAsync(T_channels, Td, ob, cudaMemcpyDeviceToHost, p->stream));
     FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));

@@ -21,6 +21,10 @@ int fz_velocity_a(int N, const FzArgs& a, const float2* H, float2* bufZ, float2*
                   float scale, cudaStream_t st);
 int fz_velocity_b(int N, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U, const float2* tw,
                   float scale, cudaStream_t st);
+int fz_terms_a(int N, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA, float2* bufB,
+               float2* Nout, const float2* tw, int* err, cudaStream_t st);
+int fz_terms_b(int N, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA, float2* bufB,
+               float2* Nout, const float2* tw, int* err, cudaStream_t st);
 int fz_tile_cols_a(int N);
 int fz_tile_cols_b(int N);
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
@@ -312,6 +316,77 @@ __global__ void __launch_bounds__(256) k_fz_reduce(const double* __restrict__ pa
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += ws[w];
     Td[(long)(a.med[b] - 1) * a.nsh + n] = r;
   }
+}
+
+// ---- live-box helpers shared with the batched partial fluxes -----------------------------------
+bool fz_box_ok(const fit_plan* p) { return fused_ok(p); }
+
+void fz_box_dims(const fit_plan* p, FzArgs* a) {
+  const GridDesc& g = p->g;
+  const int N = g.N[0];
+  memset(a, 0, sizeof(*a));
+  a->K = (p->dealias == 1) ? N / 3 - 1 : N / 2;
+  a->KX = a->K + 1;
+  a->KY = 2 * a->K + 1;
+  a->P1 = (long)a->KX * a->KY;
+  a->L = (long)g.M[0] * g.M[0];
+  a->nsh = p->nsh;
+  a->so = (float)(g.padded ? (double)g.Mtot / ((double)g.Ntot * (double)g.Ntot) : 1.0 / (double)g.Ntot);
+}
+
+// H (Hermitian part of the masked field F), the effective carrier of `inv` and the two shell maps on
+// the live box (layouts [c][kz'][col] and [kz'][col]).
+int fz_box_setup(fit_plan* p, const FzArgs& a, const void* F, int inv, float2* H, float2* Ceff, uint16_t* seff,
+                 uint16_t* sb) {
+  const GridDesc& g = p->g;
+  const long nset = a.P1 * a.KY;
+  fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
+  if (p->io_f64)
+    k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
+        g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
+        seff, sb);
+  else
+    k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
+        g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
+        seff, sb);
+  fit_prof_end(p->stream);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+// Derivative multipliers of the live indices f + K (host-computed, the +N/2 padded rule as the
+// generic path), copied to kd (KY floats; never during a capture).
+int fz_box_kd(fit_plan* p, const FzArgs& a, float* kd) {
+  const GridDesc& g = p->g;
+  const int N = g.N[0];
+  std::vector<float> h(a.KY);
+  const std::vector<double>& ks = p->ks_host[0];
+  for (int i = 0; i < a.KY; ++i) {
+    const int f = i - a.K;
+    double v = ks[((f % N) + N) % N];
+    if (g.padded && 2 * f == N) v = -ks[N / 2];
+    h[i] = (float)v;
+  }
+  FIT_CUDA_CHECK(cudaMemcpy(kd, h.data(), sizeof(float) * a.KY, cudaMemcpyHostToDevice));
+  return FIT_OK;
+}
+
+int fz_box_velocity(fit_plan* p, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U) {
+  const int M = p->g.M[0];
+  const float sc = (float)(1.0 / ((double)p->g.Mtot * (double)p->g.Mtot));
+  int rc = fz_velocity_a(M, a, H, bufZ, bufY, U, p->ax[0].tw32, sc, p->stream);
+  if (rc == 1) rc = fz_velocity_b(M, a, H, bufZ, bufY, U, p->ax[0].tw32, sc, p->stream);
+  if (rc == 1) fit_set_error("no fused kernels for size %d", M);
+  return rc == 1 ? FIT_ERR_SIZE : rc;
+}
+
+int fz_box_terms(fit_plan* p, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA,
+                 float2* bufB, float2* Nout, int* err) {
+  const int M = p->g.M[0];
+  int rc = fz_terms_a(M, a, H, kd, U, bufA, bufB, Nout, p->ax[0].tw32, err, p->stream);
+  if (rc == 1) rc = fz_terms_b(M, a, H, kd, U, bufA, bufB, Nout, p->ax[0].tw32, err, p->stream);
+  if (rc == 1) fit_set_error("no fused kernels for size %d", M);
+  return rc == 1 ? FIT_ERR_SIZE : rc;
 }
 
 static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {

@@ -96,3 +96,21 @@ def test_errors():
     u3, ks3 = curl_noise_3d(8, 1)
     with pytest.raises(ValueError):
         F.calculate_partial_fluxes_multi(u3, ks3, invariants=[F.PassiveScalar()])
+
+
+@pytest.mark.parametrize("deal", ["two_thirds", "three_halves"])
+def test_live_box_form_64(deal):
+    """FP32 cubic plans of a fused transform size take the live-box form (the four terms as one
+    batch of whole-box passes, one binning pass); against the oracle, eager, captured and replayed.
+    (The Helmholtz split is 2D-only, as in the reference, so only the helical form reaches it.)"""
+    u, ks = curl_noise_3d(64, 13)
+    invs = ((F.KineticEnergy(), "ke"), (F.Helicity(), "helicity"))
+    runs = []
+    for _ in range(3):
+        runs.append(F.calculate_partial_fluxes_multi(u, ks, invariants=[i for i, _ in invs],
+                                                     binning=F.LinearBinning(1.0), dealiasing=DEAL[deal],
+                                                     spectral=F.GB300Spectral(32)))
+    _check(runs[-1], u, ks, "helical", deal, invs, 32)
+    for name in runs[0]:
+        for key, c in runs[0][name].channels.items():
+            assert np.array_equal(runs[2][name].channels[key].transfer_spectrum, c.transfer_spectrum)
