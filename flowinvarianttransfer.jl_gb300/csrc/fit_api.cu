@@ -545,6 +545,9 @@ int fit_spectral_flux(fit_plan* p, const void* u_hat, const void* adv_hat, const
     FIT_TRY(nonlinear_half<double>(p, ud, ad, 0, false));
     FIT_TRY(carrier_and_bin_setup<double>(p, cd, invariant));
     FIT_TRY(bin_into<double>(p, p->nh.p, 0, 1, p->ceff.p, Td));
+  } else if (fz_box_ok(p)) {   // FP32 cubic 3D of a fused size: the nonlinear term on the live box
+    FIT_TRY(s2s_box_flux(p, ud, ad, cd, invariant, Td));
+    FIT_TRY(s2s_check(p));
   } else {
     FIT_TRY(nonlinear_half<float>(p, ud, ad, 0, false));
     FIT_TRY(carrier_and_bin_setup<float>(p, cd, invariant));

@@ -46,7 +46,7 @@ struct S2SState {
   std::vector<int> ext;   // per shell: largest |signed frequency| along x, y, z
   fit_dbuf occ_dev;
   // fused-path buffers
-  fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr;
+  fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr, fN;   // fN: the live-box N̂ of the flux form
   int fkd_n = -1;
   // per (band shell, pencil tile) lists of the shell's live modes (zinv inputs), rebuilt when the
   // shell table changes
@@ -62,7 +62,7 @@ void s2s_free(fit_plan* p) {
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
   fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse,  &s->fsb,  &s->fkd,  &s->fA,
-                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill};
+                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill, &s->fN};
   for (fit_dbuf* b : bufs)
     if (b->p) cudaFree(b->p);
   delete s;
@@ -527,6 +527,63 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     FIT_LAUNCH_CHECK();
   }
   return FIT_OK;
+}
+
+// Spectral flux T(n) = sum over shell n of Re(conj(C) N), N = (a . grad) u, on the live box for FP32
+// cubic 3D plans of a fused size: H of u (and of a, when it differs), the carrier of `inv` from c,
+// a in physical space, N as one whole-box term through the fused passes, one binning pass.
+int s2s_box_flux(fit_plan* p, const void* ud, const void* ad, const void* cd, int inv, double* Td) {
+  S2SState* s = (S2SState*)p->s2s;
+  if (!s) {
+    s = new S2SState();
+    p->s2s = s;
+  }
+  const GridDesc& g = p->g;
+  FzArgs a;
+  fz_box_dims(p, &a);
+  const long BL = (long)a.KY * a.P1;
+  const double M = g.M[0];
+  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
+  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 6 * BL));
+  FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * BL));
+  FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * BL));
+  FIT_TRY(ensure(p, &s->fsb, sizeof(uint16_t) * BL));
+  FIT_TRY(ensure(p, &s->fkd, sizeof(float) * a.KY));
+  FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA)));
+  FIT_TRY(ensure(p, &s->fB, (size_t)(8.0 * perB)));
+  FIT_TRY(ensure(p, &s->fN, sizeof(float2) * 3 * BL));
+  FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
+  if (!s->ferr.p) {
+    FIT_TRY(ensure(p, &s->ferr, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(s->ferr.p, 0, sizeof(int)));
+  }
+  if (s->fkd_n != a.KY) {
+    FIT_TRY(fz_box_kd(p, a, (float*)s->fkd.p));
+    s->fkd_n = a.KY;
+  }
+  float2* H = (float2*)s->fH.p;
+  float2* Ce = (float2*)s->fC.p;
+  uint16_t* se = (uint16_t*)s->fse.p;
+  uint16_t* sb = (uint16_t*)s->fsb.p;
+  if (cd != ud) FIT_TRY(fz_box_setup(p, a, cd, inv, H, Ce, se, sb));   // carrier (H overwritten below)
+  FIT_TRY(fz_box_setup(p, a, ud, inv, H, cd == ud ? Ce : (float2*)s->fN.p, se, sb));
+  const float2* Ha = H;
+  if (ad != ud) {
+    FIT_TRY(fz_box_setup(p, a, ad, inv, H + 3 * BL, (float2*)s->fN.p, se, sb));
+    Ha = H + 3 * BL;
+  }
+  FIT_TRY(fz_box_velocity(p, a, Ha, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p));
+  a.nb = 1;
+  a.ext[0][0] = a.ext[0][1] = a.ext[0][2] = (short)a.K;
+  FIT_TRY(fz_box_terms(p, a, H, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p, (float2*)s->fB.p,
+                       (float2*)s->fN.p, (int*)s->ferr.p));
+  BinOut o;
+  o.p[0] = Td;
+  const long cap = 2L * 152 * p->nsh;
+  FIT_TRY(ensure(p, &p->partial, sizeof(double) * cap));
+  return bin_density_multi<float>(g, (const float2*)s->fN.p, 3 * BL, 1, Ce, 3 * BL, 1, 3, se, p->nsh,
+                                  (double*)p->partial.p, cap, o, p->stream, BL);
 }
 
 static int run_s2s(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {

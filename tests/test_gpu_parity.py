@@ -104,6 +104,22 @@ def test_spectral_flux_3d_non_hermitian(inv, dims):
     assert rel(r.transfer_spectrum, T) < 1e-11
 
 
+@pytest.mark.parametrize("inv", ["ke", "helicity", "enstrophy"])
+@pytest.mark.parametrize("deal", ["two_thirds", "three_halves"])
+@pytest.mark.parametrize("adv", [False, True])
+def test_spectral_flux_live_box_fp32(inv, deal, adv):
+    """FP32 cubic plans of a fused transform size compute the flux's nonlinear term on the live box
+    (self-advection and a separate advecting field), against the FP64 oracle."""
+    F.clear_plans()
+    u, ks = curl_noise_3d(64, 43)
+    a = curl_noise_3d(64, 44)[0] if adv else None
+    I = {"ke": F.KineticEnergy(), "helicity": F.Helicity(), "enstrophy": F.Enstrophy()}[inv]
+    r = F.calculate_spectral_flux(u, ks, binning=F.LinearBinning(2.0), invariant=I, dealiasing=DEAL[deal],
+                                  spectral=F.GB300Spectral(32), advecting_hat=a)
+    _, T, _ = O.spectral_flux(u, ks, ("linear", 2.0), deal, inv, adv_hat=a)
+    assert rel(r.transfer_spectrum, T) < 2e-5
+
+
 def test_scalar_flux_and_decomposed_flux():
     u, ks = solenoidal_2d(16, 32)
     th = scalar_2d(16, 33)
