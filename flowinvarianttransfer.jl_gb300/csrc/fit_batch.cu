@@ -49,9 +49,13 @@ __global__ void k_cumsum(const double* __restrict__ T, double* __restrict__ Pi, 
 
 template <typename T>
 static int flux_device(fit_plan* p, const fit_batch_inst& in) {
-  FIT_TRY(nonlinear_half<T>(p, in.u, in.a, 0, false));
-  FIT_TRY(carrier_and_bin_setup<T>(p, in.u, in.inv));
-  FIT_TRY(bin_into<T>(p, p->nh.p, 0, 1, p->ceff.p, in.T));
+  if (sizeof(T) == 4 && fz_box_ok(p)) {   // FP32 cubic 3D of a fused size: the live-box form
+    FIT_TRY(s2s_box_flux(p, in.u, in.a ? in.a : in.u, in.u, in.inv, in.T));
+  } else {
+    FIT_TRY(nonlinear_half<T>(p, in.u, in.a, 0, false));
+    FIT_TRY(carrier_and_bin_setup<T>(p, in.u, in.inv));
+    FIT_TRY(bin_into<T>(p, p->nh.p, 0, 1, p->ceff.p, in.T));
+  }
   if (in.Pi) {
     k_cumsum<<<1, 32, 0, p->stream>>>(in.T, in.Pi, p->nsh);
     FIT_LAUNCH_CHECK();
