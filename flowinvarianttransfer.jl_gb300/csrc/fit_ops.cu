@@ -504,13 +504,17 @@ FIT_D void st_c(void* p, int f64, long i, double2 v) {
 // Arithmetic in CT: FP32 for single-precision fields, FP64 otherwise. The split is invariant under
 // the choice of the transverse pair (e1, e2): a rotation of the pair multiplies h+- by a phase and
 // the coefficients by its conjugate.
+// kept_only: modes outside the 2/3-kept box are neither read nor written (for consumers that
+// never read them).
 template <typename CT>
-__global__ void __launch_bounds__(256) k_helical(GridDesc g, KTab kt, const void* u, int f64, void* up, void* um) {
+__global__ void __launch_bounds__(256) k_helical(GridDesc g, KTab kt, const void* u, int f64, void* up, void* um,
+                                                 int kept_only) {
   typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= g.Ntot) return;
   int k[3];
   decode_full(g, i, k);
+  if (kept_only && !keep23(g, k)) return;
   const CT kx = ktab_at<CT>(kt, 0, k[0]), ky = ktab_at<CT>(kt, 1, k[1]), kz = ktab_at<CT>(kt, 2, k[2]);
   const CT kk = sqrt(kx * kx + ky * ky + kz * kz);
   const long n = g.Ntot;
@@ -554,13 +558,14 @@ __global__ void __launch_bounds__(256) k_helical(GridDesc g, KTab kt, const void
   }
 }
 
-int helical_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* up, void* um, cudaStream_t st) {
+int helical_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* up, void* um, cudaStream_t st,
+                  bool kept_only) {
   if (g.nd != 3) {
     fit_set_error("HelicalDecomposition is defined in 3D only (got nd=%d).", g.nd);
     return FIT_ERR_ARG;
   }
-  if (in_f64) k_helical<double><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um);
-  else k_helical<float><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um);
+  if (in_f64) k_helical<double><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um, kept_only ? 1 : 0);
+  else k_helical<float><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, up, um, kept_only ? 1 : 0);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }

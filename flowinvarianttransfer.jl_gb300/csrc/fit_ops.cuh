@@ -149,7 +149,8 @@ int density_full(const GridDesc& g, const KTab& kt, const void* carrier, const v
 
 // Helical (Craya-Herring) split of a 3D field on the full N grid (src/Decomposition.jl:63-98).
 int helical_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* up, void* um,
-                  cudaStream_t st);
+                  cudaStream_t st,
+                  bool kept_only = false);
 // Rotational / divergent (spectral Leray) split of a 2D field.
 int helmholtz_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* rot, void* div,
                     cudaStream_t st);

@@ -24,7 +24,7 @@ namespace fit {
 bool fz_box_ok(const fit_plan* p);
 void fz_box_dims(const fit_plan* p, FzArgs* a);
 int fz_box_setup(fit_plan* p, const FzArgs& a, const void* F, int inv, float2* H, float2* Ceff, uint16_t* seff,
-                 uint16_t* sb);
+                 uint16_t* sb, int inv2, float2* Ceff2);
 int fz_box_kd(fit_plan* p, const FzArgs& a, float* kd);
 int fz_box_velocity(fit_plan* p, const FzArgs& a, const float2* H, float2* bufZ, float2* bufY, float* U);
 int fz_box_terms(fit_plan* p, const FzArgs& a, const float2* H, const float* kd, const float* U, float2* bufA,
@@ -133,7 +133,8 @@ static int run_partial_box(fit_plan* p, PartialState* s, const void* ud, int dec
   const size_t cb = (p->io_f64 ? 16 : 8) * (size_t)g.Ntot * 3;
   FIT_TRY(pbuf(p, &s->comp, 2 * cb));
   void* comp[2] = {s->comp.p, (char*)s->comp.p + cb};
-  if (decomposition == FIT_DECOMP_HELICAL) FIT_TRY(helical_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
+  if (decomposition == FIT_DECOMP_HELICAL) FIT_TRY(helical_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream,
+                                                             p->dealias == 1));
   else FIT_TRY(helmholtz_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
   FzArgs a;
   fz_box_dims(p, &a);
@@ -160,10 +161,11 @@ static int run_partial_box(fit_plan* p, PartialState* s, const void* ud, int dec
   }
   float2* H = (float2*)s->bH.p;
   float2* Cf = (float2*)s->bC.p;
-  for (int sk = 0; sk < 2; ++sk)
-    for (int j = 0; j < ninv; ++j)
+  for (int sk = 0; sk < 2; ++sk)   // H_sk and the carriers of two invariants per pass over the field
+    for (int j = 0; j < ninv; j += 2)
       FIT_TRY(fz_box_setup(p, a, comp[sk], invs[j], H + (long)sk * 3 * BL, Cf + (long)(j * 2 + sk) * 3 * BL,
-                           (uint16_t*)s->bse.p, (uint16_t*)s->bsb.p));
+                           (uint16_t*)s->bse.p, (uint16_t*)s->bsb.p, j + 1 < ninv ? invs[j + 1] : -1,
+                           j + 1 < ninv ? Cf + (long)((j + 1) * 2 + sk) * 3 * BL : nullptr));
   float* U = (float*)s->bU.p;
   for (int sp = 0; sp < 2; ++sp)
     FIT_TRY(fz_box_velocity(p, a, H + (long)sp * 3 * BL, (float2*)s->bA.p, (float2*)s->bB.p,

@@ -215,7 +215,7 @@ template <typename CT>
 __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, const void* F,
                                                   int f64, int inv, int two_thirds,
                                                   const uint16_t* __restrict__ shell, float2* H, float2* Ceff,
-                                                  uint16_t* seff, uint16_t* sb) {
+                                                  uint16_t* seff, uint16_t* sb, int inv2, float2* Ceff2) {
   typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= P1 * KY) return;
@@ -249,6 +249,17 @@ __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, in
   for (int c = 0; c < 3; ++c)
     Ceff[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
   seff[(long)kz * P1 + col] = sh;
+  if (Ceff2) {   // a second invariant's carrier from the same field
+#pragma unroll
+    for (int c = 0; c < 3; ++c) CA[c] = CB[c] = mkc<C2>(0, 0);
+    if (sh) {
+      if (A) carrier_at_t<CT>(g, kt, F, f64, g.Ntot, 3, inv2, kA.lin, kA.k, CA);
+      if (B) carrier_at_t<CT>(g, kt, F, f64, g.Ntot, 3, inv2, kB.lin, kB.k, CB);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      Ceff2[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
+  }
 }
 
 // Mode lists of the z pass: count the live modes of every (band shell, pencil tile), scan the
@@ -337,18 +348,18 @@ void fz_box_dims(const fit_plan* p, FzArgs* a) {
 // H (Hermitian part of the masked field F), the effective carrier of `inv` and the two shell maps on
 // the live box (layouts [c][kz'][col] and [kz'][col]).
 int fz_box_setup(fit_plan* p, const FzArgs& a, const void* F, int inv, float2* H, float2* Ceff, uint16_t* seff,
-                 uint16_t* sb) {
+                 uint16_t* sb, int inv2, float2* Ceff2) {
   const GridDesc& g = p->g;
   const long nset = a.P1 * a.KY;
   fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
   if (p->io_f64)
     k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
         g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
-        seff, sb);
+        seff, sb, inv2, Ceff2);
   else
     k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
         g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
-        seff, sb);
+        seff, sb, inv2, Ceff2);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
@@ -439,10 +450,10 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
   if (p->io_f64)
     k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
-        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp);
+        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr);
   else
     k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
-        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp);
+        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   const int ntile = (int)npt;
@@ -566,11 +577,11 @@ int s2s_box_flux(fit_plan* p, const void* ud, const void* ad, const void* cd, in
   float2* Ce = (float2*)s->fC.p;
   uint16_t* se = (uint16_t*)s->fse.p;
   uint16_t* sb = (uint16_t*)s->fsb.p;
-  if (cd != ud) FIT_TRY(fz_box_setup(p, a, cd, inv, H, Ce, se, sb));   // carrier (H overwritten below)
-  FIT_TRY(fz_box_setup(p, a, ud, inv, H, cd == ud ? Ce : (float2*)s->fN.p, se, sb));
+  if (cd != ud) FIT_TRY(fz_box_setup(p, a, cd, inv, H, Ce, se, sb, -1, nullptr));   // carrier (H overwritten below)
+  FIT_TRY(fz_box_setup(p, a, ud, inv, H, cd == ud ? Ce : (float2*)s->fN.p, se, sb, -1, nullptr));
   const float2* Ha = H;
   if (ad != ud) {
-    FIT_TRY(fz_box_setup(p, a, ad, inv, H + 3 * BL, (float2*)s->fN.p, se, sb));
+    FIT_TRY(fz_box_setup(p, a, ad, inv, H + 3 * BL, (float2*)s->fN.p, se, sb, -1, nullptr));
     Ha = H + 3 * BL;
   }
   FIT_TRY(fz_box_velocity(p, a, Ha, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p));
