@@ -191,78 +191,107 @@ static int forward_spectrum(fit_plan* p, const void* u_dev, void* out_dev) {
 
 // ---- forced Navier-Stokes ---------------------------------------------------------------------
 
-FIT_D void ns_k(const GridDesc& g, const KTab& kt, long i, double* kv, int* kidx) {
-  kidx[0] = (int)(i % g.N[0]);
-  const long r = i / g.N[0];
-  kidx[1] = (int)(r % g.N[1]);
-  kidx[2] = (int)(r / g.N[1]);
-  for (int d = 0; d < 3; ++d) kv[d] = d < g.nd ? kt.k[d][kidx[d]] : 0.0;
-}
-
-__global__ void k_ns_forced_energy(GridDesc g, KTab kt, const void* u, int f64, int nc, double kf, double* ef) {
-  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+// Energy of the forced band 0 < |k| <= kf, summed in FP64 over the modes of a box of signed
+// indices lo_d .. lo_d + len_d - 1 per axis that holds every |k_d| <= kf (each index once): only that
+// corner of the spectrum is read.
+template <typename CT>
+__global__ void k_ns_forced_energy(GridDesc g, KTab kt, const void* u, int f64, int nc, double kf, int3 lo, int3 len,
+                                   double* ef) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   double e = 0.0;
-  if (i < g.Ntot) {
-    double kv[3];
-    int kidx[3];
-    ns_k(g, kt, i, kv, kidx);
-    const double k2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
-    if (k2 > 0.0 && k2 <= kf * kf)
-      for (int c = 0; c < nc; ++c) {
-        const double2 v = ld_c(u, f64, i + g.Ntot * c);
-        e += 0.5 * (v.x * v.x + v.y * v.y);
-      }
+  if (t < len.x * len.y * len.z) {
+    int k[3] = {t % len.x + lo.x, (t / len.x) % len.y + lo.y, t / (len.x * len.y) + lo.z};
+    {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) k[d] = k[d] < 0 ? k[d] + g.N[d] : k[d];
+      double k2 = 0.0;   // the band test in FP64, as the reference's
+      for (int d = 0; d < g.nd; ++d) k2 += kt.k[d][k[d]] * kt.k[d][k[d]];
+      const long i = k[0] + (long)g.N[0] * (k[1] + (long)g.N[1] * k[2]);
+      if (k2 > 0.0 && k2 <= kf * kf)
+        for (int c = 0; c < nc; ++c) {
+          const double2 v = ld_c(u, f64, i + g.Ntot * c);
+          e += 0.5 * (v.x * v.x + v.y * v.y);
+        }
+    }
   }
   for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
   __shared__ double ws[32];
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = e;
   __syncthreads();
   if (threadIdx.x < 32) {
-    double s = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (threadIdx.x == 0) atomicAdd(ef, s);
+    double sum = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (threadIdx.x == 0) atomicAdd(ef, sum);
   }
 }
 
 // out = a*u0 + b*(uin + dt*L(uin)), L = -P[N] - nu k^2 uin + alpha uin [0<|k|<=kf]; the state is
-// restricted to the retained (2/3) modes.
+// restricted to the retained (2/3) modes. CT: FP32 for single-precision fields (per-mode work, no
+// sums), FP64 otherwise.
+template <typename CT>
 __global__ void k_ns_update(GridDesc g, KTab kt, const void* u0, const void* uin, const void* Nh, void* out, int f64,
                             int nc, double a, double b, double dt, double nu, double kf, double power,
-                            const double* ef, int two_thirds, double nscale) {
+                            const double* ef, int two_thirds, double nscale, int3 fm) {
+  typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= g.Ntot) return;
-  double kv[3];
   int kidx[3];
-  ns_k(g, kt, i, kv, kidx);
-  const double k2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+  decode_full(g, i, kidx);
+  CT kv[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) kv[d] = d < g.nd ? ktab_at<CT>(kt, d, kidx[d]) : (CT)0;
+  const CT k2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
   const bool keep = !two_thirds || keep23(g, kidx);
-  double2 nn[3], ui[3];
-  double kn_re = 0.0, kn_im = 0.0;
-  for (int c = 0; c < nc; ++c) {
-    nn[c] = ld_c(Nh, f64, i + g.Ntot * c);
-    nn[c].x *= nscale;
-    nn[c].y *= nscale;
-    ui[c] = ld_c(uin, f64, i + g.Ntot * c);
+  C2 nn[3], ui[3];
+  CT kn_re = 0, kn_im = 0;
+  const CT ns = (CT)nscale;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (c >= nc) break;
+    nn[c] = ld_ct<CT>(Nh, f64, i + g.Ntot * c);
+    nn[c].x *= ns;
+    nn[c].y *= ns;
+    ui[c] = ld_ct<CT>(uin, f64, i + g.Ntot * c);
     kn_re += kv[c] * nn[c].x;
     kn_im += kv[c] * nn[c].y;
   }
-  const double alpha = (k2 > 0.0 && k2 <= kf * kf && *ef > 0.0) ? power / (2.0 * *ef) : 0.0;
-  for (int c = 0; c < nc; ++c) {
-    double2 pn = nn[c];
-    if (k2 > 0.0) {
+  // forcing band 0 < |k| <= kf, tested in FP64 for the modes of its index box (|signed index| <= fm)
+  bool forced = false;
+  {
+    const int fmv[3] = {fm.x, fm.y, fm.z};
+    bool inbox = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int sd = 2 * kidx[d] < g.N[d] ? kidx[d] : kidx[d] - g.N[d];
+      inbox = inbox && (sd <= fmv[d] && -sd <= fmv[d]);
+    }
+    if (inbox) {
+      double kd2 = 0.0;
+      for (int d = 0; d < g.nd; ++d) kd2 += kt.k[d][kidx[d]] * kt.k[d][kidx[d]];
+      forced = kd2 > 0.0 && kd2 <= kf * kf;
+    }
+  }
+  const CT alpha = (forced && *ef > 0.0) ? (CT)(power / (2.0 * *ef)) : (CT)0;
+  const CT cb = (CT)b, cdt = (CT)dt, ca = (CT)a;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (c >= nc) break;
+    C2 pn = nn[c];
+    if (k2 > (CT)0) {
       pn.x -= kv[c] * kn_re / k2;
       pn.y -= kv[c] * kn_im / k2;
     }
-    const double fac = -nu * k2 + alpha;
-    double2 L = make_double2(-pn.x + fac * ui[c].x, -pn.y + fac * ui[c].y);
-    double2 r = make_double2(b * (ui[c].x + dt * L.x), b * (ui[c].y + dt * L.y));
+    const CT fac = -(CT)nu * k2 + alpha;
+    C2 r;
+    r.x = cb * (ui[c].x + cdt * (-pn.x + fac * ui[c].x));
+    r.y = cb * (ui[c].y + cdt * (-pn.y + fac * ui[c].y));
     if (a != 0.0) {
-      const double2 z = ld_c(u0, f64, i + g.Ntot * c);
-      r.x += a * z.x;
-      r.y += a * z.y;
+      const C2 z = ld_ct<CT>(u0, f64, i + g.Ntot * c);
+      r.x += ca * z.x;
+      r.y += ca * z.y;
     }
-    if (!keep || k2 == 0.0) r = make_double2(0.0, 0.0);
-    if (f64) reinterpret_cast<double2*>(out)[i + g.Ntot * c] = r;
+    if (!keep || k2 == (CT)0) r.x = r.y = (CT)0;
+    if (f64) reinterpret_cast<double2*>(out)[i + g.Ntot * c] = make_double2((double)r.x, (double)r.y);
     else reinterpret_cast<float2*>(out)[i + g.Ntot * c] = make_float2((float)r.x, (float)r.y);
   }
 }
@@ -270,15 +299,46 @@ __global__ void k_ns_update(GridDesc g, KTab kt, const void* u0, const void* uin
 template <typename T>
 static int ns_stage(fit_plan* p, const void* u0, const void* uin, void* out, void* Nfull, double a, double b,
                     double dt, double nu, double kf, double power, double* ef) {
-  FIT_TRY(nonlinear_half<T>(p, uin, uin, 0, false));
-  FIT_TRY(scatter_full<T>(p->g, (const typename Vec2<T>::t*)p->nh.p, p->M, p->dealias == 1, Nfull, p->io_f64,
-                          p->stream));
+  if (sizeof(T) == 4 && fz_box_ok(p)) {   // FP32 cubic 3D of a fused size: the live-box passes
+    FIT_TRY(s2s_box_nonlinear_full(p, uin, Nfull));
+  } else {
+    FIT_TRY(nonlinear_half<T>(p, uin, uin, 0, false));
+    FIT_TRY(scatter_full<T>(p->g, (const typename Vec2<T>::t*)p->nh.p, p->M, p->dealias == 1, Nfull, p->io_f64,
+                            p->stream));
+  }
   FIT_CUDA_CHECK(cudaMemsetAsync(ef, 0, sizeof(double), p->stream));
-  k_ns_forced_energy<<<cl_blk(p->g.Ntot, 256), 256, 0, p->stream>>>(p->g, p->kt, uin, p->io_f64, p->M, kf, ef);
+  int lo[3] = {0, 0, 0}, len[3] = {1, 1, 1};   // index box of the forced band, per axis
+  for (int d = 0; d < p->nd; ++d) {
+    const int N = p->g.N[d];
+    int m = 0;
+    while (m + 1 <= N / 2 && (fabs(p->ks_host[d][m + 1]) <= kf || fabs(p->ks_host[d][N - m - 1]) <= kf)) ++m;
+    if (2 * m + 1 >= N) {   // the whole axis
+      lo[d] = -(N / 2);
+      len[d] = N;
+    } else {
+      lo[d] = -m;
+      len[d] = 2 * m + 1;
+    }
+  }
+  const int nbox = len[0] * len[1] * len[2];
+  const bool f32 = sizeof(T) == 4;
+  if (f32)
+    k_ns_forced_energy<float><<<(nbox + 255) / 256, 256, 0, p->stream>>>(
+        p->g, p->kt, uin, p->io_f64, p->M, kf, make_int3(lo[0], lo[1], lo[2]), make_int3(len[0], len[1], len[2]), ef);
+  else
+    k_ns_forced_energy<double><<<(nbox + 255) / 256, 256, 0, p->stream>>>(
+        p->g, p->kt, uin, p->io_f64, p->M, kf, make_int3(lo[0], lo[1], lo[2]), make_int3(len[0], len[1], len[2]), ef);
   FIT_LAUNCH_CHECK();
-  k_ns_update<<<cl_blk(p->g.Ntot, 256), 256, 0, p->stream>>>(p->g, p->kt, u0, uin, Nfull, out, p->io_f64, p->M, a, b,
-                                                             dt, nu, kf, power, ef, p->dealias == 1,
-                                                             (double)p->g.Ntot * (double)p->g.Ntot);
+  const double nsc = (double)p->g.Ntot * (double)p->g.Ntot;
+  const int3 fm = make_int3(len[0] / 2, len[1] / 2, len[2] / 2);   // half-widths of the forced index box
+  if (f32)
+    k_ns_update<float><<<cl_blk(p->g.Ntot, 256), 256, 0, p->stream>>>(p->g, p->kt, u0, uin, Nfull, out, p->io_f64,
+                                                                      p->M, a, b, dt, nu, kf, power, ef,
+                                                                      p->dealias == 1, nsc, fm);
+  else
+    k_ns_update<double><<<cl_blk(p->g.Ntot, 256), 256, 0, p->stream>>>(p->g, p->kt, u0, uin, Nfull, out, p->io_f64,
+                                                                       p->M, a, b, dt, nu, kf, power, ef,
+                                                                       p->dealias == 1, nsc, fm);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -405,5 +465,5 @@ extern "C" int fit_ns_evolve(fit_plan* p, void* u_hat, int nsteps, double dt, do
   }
   if (ptr_kind != FIT_PTR_DEVICE) FIT_CUDA_CHECK(cudaMemcpyAsync(u_hat, u0, cb, cudaMemcpyDeviceToHost, p->stream));
   FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));
-  return FIT_OK;
+  return s2s_check(p);   // a bounded wait of the live-box x pass that gave up
 }

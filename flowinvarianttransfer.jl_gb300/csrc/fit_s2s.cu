@@ -233,10 +233,11 @@ __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, in
     if (okB) { const C2 v = ld_ct<CT>(F, f64, kB.lin + g.Ntot * c); acc.x += v.x; acc.y -= v.y; }
     H[((long)c * KY + kz) * P1 + col] = make_float2((float)((CT)0.5 * acc.x), (float)((CT)0.5 * acc.y));
   }
-  sb[(long)kz * P1 + col] = kA.lin >= 0 ? shell[kA.lin] : (kB.lin >= 0 ? shell[kB.lin] : 0);
+  // no shell table (a plain nonlinear term): every mode is in no shell, no carrier is formed
+  sb[(long)kz * P1 + col] = !shell ? 0 : (kA.lin >= 0 ? shell[kA.lin] : (kB.lin >= 0 ? shell[kB.lin] : 0));
   const bool A = kA.lin >= 0;
   const bool B = kB.lin >= 0 && kx >= 1 && (g.padded ? true : (2 * kx < g.N[0]));
-  uint16_t sh = A ? shell[kA.lin] : (B ? shell[kB.lin] : 0);
+  uint16_t sh = !shell ? 0 : (A ? shell[kA.lin] : (B ? shell[kB.lin] : 0));
   if (two_thirds && (A || B) && !keep23(g, A ? kA.k : kB.k)) sh = 0;
   C2 CA[3], CB[3];
 #pragma unroll
@@ -595,6 +596,85 @@ int s2s_box_flux(fit_plan* p, const void* ud, const void* ad, const void* cd, in
   FIT_TRY(ensure(p, &p->partial, sizeof(double) * cap));
   return bin_density_multi<float>(g, (const float2*)s->fN.p, 3 * BL, 1, Ce, 3 * BL, 1, 3, se, p->nsh,
                                   (double*)p->partial.p, cap, o, p->stream, BL);
+}
+
+// Live-box N̂ (half spectrum along x, [c][kz'][col]) -> the full data-grid spectrum in the user
+// layout (io precision): modes with kx < 0 are the conjugates of their mirrors, modes outside the
+// box (the 2/3-truncated ones) are zero.
+__global__ void k_box_to_full(GridDesc g, int K, int KX, int KY, long P1, const float2* __restrict__ nb, void* out,
+                              int f64) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= g.Ntot) return;
+  int k[3], f[3];
+  decode_full(g, i, k);
+  bool in = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    f[d] = (2 * k[d] < g.N[d]) ? k[d] : k[d] - g.N[d];
+    in = in && f[d] >= -K && f[d] <= K;
+  }
+  const bool cj = f[0] < 0;
+  if (cj) {
+    f[0] = -f[0];
+    f[1] = -f[1];
+    f[2] = -f[2];
+  }
+  const long m = (long)(f[2] + K) * P1 + f[0] + (long)KX * (f[1] + K);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float2 v = make_float2(0.f, 0.f);
+    if (in) {
+      v = nb[(long)c * KY * P1 + m];
+      if (cj) v.y = -v.y;
+    }
+    if (f64) reinterpret_cast<double2*>(out)[i + g.Ntot * c] = make_double2(v.x, v.y);
+    else reinterpret_cast<float2*>(out)[i + g.Ntot * c] = v;
+  }
+}
+
+// N̂ = FFT[(u . grad) u] of a self-advecting velocity through the live-box passes, written as the
+// full data-grid spectrum (user layout) to Nfull.
+int s2s_box_nonlinear_full(fit_plan* p, const void* ud, void* Nfull) {
+  S2SState* s = (S2SState*)p->s2s;
+  if (!s) {
+    s = new S2SState();
+    p->s2s = s;
+  }
+  const GridDesc& g = p->g;
+  FzArgs a;
+  fz_box_dims(p, &a);
+  const long BL = (long)a.KY * a.P1;
+  const double M = g.M[0];
+  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
+  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 3 * BL));
+  FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * BL));
+  FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * BL));
+  FIT_TRY(ensure(p, &s->fsb, sizeof(uint16_t) * BL));
+  FIT_TRY(ensure(p, &s->fkd, sizeof(float) * a.KY));
+  FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA)));
+  FIT_TRY(ensure(p, &s->fB, (size_t)(8.0 * perB)));
+  FIT_TRY(ensure(p, &s->fN, sizeof(float2) * 3 * BL));
+  FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
+  if (!s->ferr.p) {
+    FIT_TRY(ensure(p, &s->ferr, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(s->ferr.p, 0, sizeof(int)));
+  }
+  if (s->fkd_n != a.KY) {
+    FIT_TRY(fz_box_kd(p, a, (float*)s->fkd.p));
+    s->fkd_n = a.KY;
+  }
+  FIT_TRY(fz_box_setup(p, a, ud, INV_KE, (float2*)s->fH.p, (float2*)s->fC.p, (uint16_t*)s->fse.p, (uint16_t*)s->fsb.p,
+                       -1, nullptr));
+  FIT_TRY(fz_box_velocity(p, a, (const float2*)s->fH.p, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p));
+  a.nb = 1;
+  a.ext[0][0] = a.ext[0][1] = a.ext[0][2] = (short)a.K;
+  FIT_TRY(fz_box_terms(p, a, (const float2*)s->fH.p, (const float*)s->fkd.p, (const float*)p->ph.p,
+                       (float2*)s->fA.p, (float2*)s->fB.p, (float2*)s->fN.p, (int*)s->ferr.p));
+  k_box_to_full<<<(unsigned)((g.Ntot + 255) / 256), 256, 0, p->stream>>>(g, a.K, a.KX, a.KY, a.P1,
+                                                                        (const float2*)s->fN.p, Nfull, p->io_f64);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
 }
 
 static int run_s2s(fit_plan* p, S2SState* s, const void* ud, const void* ad, int inv, double* Td) {

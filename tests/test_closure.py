@@ -206,6 +206,18 @@ def test_forced_navier_stokes_3d(prec):
 
 
 @pytest.mark.gpu
+def test_forced_navier_stokes_3d_live_box():
+    """FP32 3D plans of a fused transform size evolve with the live-box nonlinear term."""
+    ns = (64, 64, 64)
+    ks = O.wavenumber_grid(ns, (2 * np.pi,) * 3)
+    u = O.dealias_copy(spectrum_field(ns, e_config2, seed=17, project=True)[0], ns)
+    u *= np.sqrt(0.5 / _energy(u))
+    ref = OC.ns_evolve(u, ks, 3, 5e-3, 2e-3, 2.0, 0.1)
+    got = F.evolve_forced_navier_stokes(u, ks, 3, 5e-3, 2e-3, kf=2.0, power=0.1, precision=32)
+    assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
 def test_forced_navier_stokes_2d_no_dealias():
     n = 32
     ks = O.wavenumber_grid((n, n), (2 * np.pi,) * 2)
