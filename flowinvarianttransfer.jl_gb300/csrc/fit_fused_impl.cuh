@@ -62,12 +62,12 @@ FIT_D float2 fz_muli(float2 h, float k) { return make_float2(-h.y * k, h.x * k);
 // elements per thread; MINB resident blocks per SM bound the registers.
 template <int N>
 struct FzTile {
-  static constexpr int C = N == 512 ? 8 : CtTile<float2, N>::C;
+  static constexpr int C = (N == 512 || N == 384) ? 8 : CtTile<float2, N>::C;
   static constexpr int E = C * N;
   static constexpr int EPT = E <= 8192 ? 8 : 16;
   static constexpr int NTHR = (E / EPT + 31) / 32 * 32;
   static constexpr size_t SMEM = (size_t)(E + N) * 8;
-  static constexpr int MINB = N == 512 ? 4 : CtTile<float2, N>::MINB;
+  static constexpr int MINB = (N == 512 || N == 384) ? 4 : CtTile<float2, N>::MINB;
   static constexpr int MINB_Y = MINB;     // yinv
   static constexpr int MINB_BIN = MINB;   // zfwd_bin (per-thread transfer sums stay live across transforms)
 };
