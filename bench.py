@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison")
     ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial", "padded", "m2m"],
                     help="s2s: the 512^3 shell-to-shell headline; closure: learned closure vs exact "
                          "coarse-graining flux on a forced 256^3 field; batch: 64 uneven spectral-flux "
@@ -384,6 +385,24 @@ def run_ours(args):
            "steps": args.e2e_steps, "call_ms": call_ms}
     del host, host_np
 
+    # ---- cuFFT beside, as a comparison only: the library's 3D real transforms at this size, and
+    # what the reference algorithm's transform count for one T(n,m) (3 + 12 N_sh unpruned real 3D
+    # transforms) would take on them alone ----
+    cufft = None
+    if not args.no_cufft:
+        x = torch.randn((N, N, N), dtype=torch.float32, device=dev)
+        X = torch.fft.rfftn(x)
+        t_f = _timed_ms(lambda: torch.fft.rfftn(x), stream, 5, warm=2)
+        t_i = _timed_ms(lambda: torch.fft.irfftn(X, s=(N, N, N)), stream, 5, warm=2)
+        per = 0.5 * (t_f + t_i)
+        n_t = 3 + 12 * nsh
+        cufft = {"library": "cuFFT (torch.fft, %s)" % torch.version.cuda, "rfftn_ms": t_f, "irfftn_ms": t_i,
+                 "GBps_per_transform_model": 6.0 * N ** 3 * 4 / (per / 1e3) / 1e9,
+                 "unpruned_transforms_per_T": n_t, "transforms_only_ms_per_T": n_t * per,
+                 "ours_ms_per_T": ms, "ours_vs_cufft_transforms_only": n_t * per / ms}
+        del x, X
+        torch.cuda.empty_cache()
+
     # ---- plain FP64 form (one nonlinear term per mediator) ----
     fp64 = None
     if not args.no_fp64:
@@ -442,7 +461,8 @@ def run_ours(args):
                            "seed": args.seed, "parallelism": f"replicas x{ws}",
                            "l2": "inputs 3.2 GB per step >> 129 MB L2; no flush needed"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches / args.steps),
-                "gpu_launches_timed_region": int(launches), "clocks": clocks, "fp64_plain": fp64}
+                "gpu_launches_timed_region": int(launches), "clocks": clocks, "fp64_plain": fp64,
+                "cufft_comparison": cufft}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
