@@ -12,7 +12,7 @@ from . import _build
 EXPORTS = [
     "fit_plan_create", "fit_plan_destroy", "fit_last_error", "fit_plan_set_stream", "fit_plan_info",
     "fit_launch_count", "fit_nonlinear_term", "fit_assign_shells", "fit_transfer_density",
-    "fit_spectral_flux", "fit_shell_to_shell", "fit_helical_decompose", "fit_helmholtz_decompose",
+    "fit_spectral_flux", "fit_shell_to_shell", "fit_helical_decompose", "fit_helmholtz_decompose", "fit_toroidal_poloidal_decompose",
     "fit_partial_fluxes", "fit_mode_to_mode", "fit_prof_enable", "fit_prof_read", "fit_prof_kind_name",
     "fit_coarse_graining_flux", "fit_forward_spectrum", "fit_ns_evolve", "fit_mlp_nparams", "fit_mlp_forward", "fit_mlp_status",
     "fit_mlp_train_grad", "fit_mlp_adam", "fit_gradient_model_flux", "fit_field_moments", "fit_field_compare",
@@ -49,6 +49,7 @@ def _declare(lib):
     lib.fit_spectral_flux.argtypes = [vp, vp, vp, vp, dp, i32, u32, i32, i32, vp, vp, i32]
     lib.fit_shell_to_shell.argtypes = [vp, vp, vp, dp, i32, u32, i32, i32, i32, i32, vp, vp, vp, i32]
     lib.fit_helical_decompose.argtypes = [vp, vp, vp, vp, i32]
+    lib.fit_toroidal_poloidal_decompose.argtypes = [vp, vp, vp, vp, i32]
     lib.fit_helmholtz_decompose.argtypes = [vp, vp, vp, vp, i32]
     lib.fit_partial_fluxes.argtypes = [vp, vp, i32, i32, dp, i32, u32, i32, vp, i32]
     lib.fit_mode_to_mode.argtypes = [vp, vp, vp, i32, i32, vp, vp, i32]

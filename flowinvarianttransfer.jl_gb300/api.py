@@ -17,7 +17,8 @@ from .types import (BandToBandResult, DivergentDecomposition, DirectSumBackend, 
                     GB300Spectral, HelicalDecomposition, HelmholtzDecomposition, Helicity, IsotropicShells,
                     KineticEnergy, ModeToModeTransferMethod, ModeToModeTriadResult, NoDecomposition,
                     OrszagTwoThirds, PaddedThreeHalves, PartialFluxResult, PassiveScalar, RotationalDecomposition,
-                    ShellToShellResult, ShellToShellTransferMethod, SpectralFluxMethod, SpectralFluxResult)
+                    ShellToShellResult, ShellToShellTransferMethod, SpectralFluxMethod, SpectralFluxResult,
+                    ToroidalPoloidalDecomposition)
 
 
 def _spec_precision(spectral, arr):
@@ -82,7 +83,7 @@ def transfer_density(invariant, velocity_hat, N_hat, ks):
 
 # ---- decompositions ------------------------------------------------------------------------------
 def decompose_field(decomposition, velocity_hat, ks):
-    """``decompose_field`` on spectral data (``src/Decomposition.jl:38-98``)."""
+    """``decompose_field`` on spectral data (``src/Decomposition.jl:38-141``)."""
     v = np.asarray(velocity_hat)
     if isinstance(decomposition, NoDecomposition):
         return v
@@ -90,6 +91,9 @@ def decompose_field(decomposition, velocity_hat, ks):
     if isinstance(decomposition, HelicalDecomposition):
         up, um = p.helical(v)
         return {"positive": up.astype(v.dtype), "negative": um.astype(v.dtype)}
+    if isinstance(decomposition, ToroidalPoloidalDecomposition):
+        t, q = p.toroidal_poloidal(v)
+        return {"toroidal": t.astype(v.dtype), "poloidal": q.astype(v.dtype)}
     if isinstance(decomposition, (HelmholtzDecomposition, RotationalDecomposition, DivergentDecomposition)):
         r, d = p.helmholtz(v)
         if isinstance(decomposition, RotationalDecomposition):
@@ -181,6 +185,8 @@ def _decomposition_code(decomposition):
         return 1, HelicalDecomposition.names
     if isinstance(decomposition, HelmholtzDecomposition):
         return 2, HelmholtzDecomposition.names
+    if isinstance(decomposition, ToroidalPoloidalDecomposition):
+        return 3, ToroidalPoloidalDecomposition.names
     raise ValueError("calculate_partial_fluxes needs a decomposition that splits u into ≥2 named components "
                      f"(e.g. HelicalDecomposition or HelmholtzDecomposition); got {type(decomposition).__name__}.")
 

@@ -659,6 +659,28 @@ int fit_helical_decompose(fit_plan* p, const void* u_hat, void* up, void* um, in
   return sync_plan(p);
 }
 
+int fit_toroidal_poloidal_decompose(fit_plan* p, const void* u_hat, void* tor, void* pol, int ptr_kind) {
+  API_CHECK(p != nullptr && u_hat != nullptr && tor != nullptr && pol != nullptr, FIT_ERR_ARG, "NULL argument");
+  API_CHECK(p->nd == 3, FIT_ERR_ARG, "ToroidalPoloidalDecomposition is defined in 3D only (got nd=%d).", p->nd);
+  API_CHECK(p->M >= 3, FIT_ERR_ARG, "ToroidalPoloidalDecomposition needs >=3 velocity components (got D=%d).", p->M);
+  const size_t fb = cbytes(p) * p->g.Ntot * 3;
+  const void* ud;
+  FIT_TRY(stage_in(p, &p->in_u, u_hat, cbytes(p) * p->g.Ntot * p->M, ptr_kind, &ud));
+  void *a = tor, *b = pol;
+  if (ptr_kind != FIT_PTR_DEVICE) {
+    FIT_TRY(ensure(p, &p->out_c, fb));
+    FIT_TRY(ensure(p, &p->out_c2, fb));
+    a = p->out_c.p;
+    b = p->out_c2.p;
+  }
+  FIT_TRY(toroidal_split(p->g, p->kt, ud, p->io_f64, a, b, p->stream));
+  if (ptr_kind != FIT_PTR_DEVICE) {
+    FIT_TRY(copy_out(p, tor, a, fb, ptr_kind));
+    FIT_TRY(copy_out(p, pol, b, fb, ptr_kind));
+  }
+  return sync_plan(p);
+}
+
 int fit_helmholtz_decompose(fit_plan* p, const void* u_hat, void* ur, void* udv, int ptr_kind) {
   API_CHECK(p != nullptr && u_hat != nullptr && ur != nullptr && udv != nullptr, FIT_ERR_ARG, "NULL argument");
   API_CHECK(p->nd == 2 && p->M == 2, FIT_ERR_ARG, "Helmholtz decomposition currently supports 2D fields only.");
@@ -683,8 +705,9 @@ int fit_helmholtz_decompose(fit_plan* p, const void* u_hat, void* ur, void* udv,
 int fit_partial_fluxes(fit_plan* p, const void* u_hat, int decomposition, int invariant, const double* edges,
                        int n_edges, uint32_t dims_mask, int coord_f32, double* T_channels, int ptr_kind) {
   API_CHECK(p != nullptr && u_hat != nullptr && T_channels != nullptr, FIT_ERR_ARG, "NULL argument");
-  API_CHECK(decomposition == FIT_DECOMP_HELICAL || decomposition == FIT_DECOMP_HELMHOLTZ, FIT_ERR_ARG,
-            "calculate_partial_fluxes needs a decomposition that splits u into >=2 named components");
+  API_CHECK(decomposition == FIT_DECOMP_HELICAL || decomposition == FIT_DECOMP_HELMHOLTZ ||
+                decomposition == FIT_DECOMP_TOROIDAL_POLOIDAL,
+            FIT_ERR_ARG, "calculate_partial_fluxes needs a decomposition that splits u into >=2 named components");
   API_CHECK(p->M == p->nd && p->Dadv == p->nd, FIT_ERR_ARG, "partial fluxes need an nd-component velocity plan");
   FIT_TRY(check_invariant(p, invariant, p->M));
   const size_t fb = cbytes(p) * p->g.Ntot * p->M;
@@ -693,6 +716,8 @@ int fit_partial_fluxes(fit_plan* p, const void* u_hat, int decomposition, int in
   FIT_TRY(ensure(p, &p->out_c, fb));
   FIT_TRY(ensure(p, &p->out_c2, fb));
   if (decomposition == FIT_DECOMP_HELICAL) FIT_TRY(helical_split(p->g, p->kt, ud, p->io_f64, p->out_c.p, p->out_c2.p, p->stream));
+  else if (decomposition == FIT_DECOMP_TOROIDAL_POLOIDAL)
+    FIT_TRY(toroidal_split(p->g, p->kt, ud, p->io_f64, p->out_c.p, p->out_c2.p, p->stream));
   else FIT_TRY(helmholtz_split(p->g, p->kt, ud, p->io_f64, p->out_c.p, p->out_c2.p, p->stream));
   const void* comp[2] = {p->out_c.p, p->out_c2.p};
   FIT_TRY(ensure_shells(p, edges, n_edges, dims_mask, coord_f32));

@@ -558,6 +558,75 @@ __global__ void __launch_bounds__(256) k_helical(GridDesc g, KTab kt, const void
   }
 }
 
+// Toroidal / poloidal split per mode, as src/Decomposition.jl:107-141: e1 = khat x zhat normalised
+// (horizontal, toroidal direction), e2 = khat x e1 (poloidal); for k parallel to zhat the pair is
+// (xhat, yhat); tor = (u . e1) e1, pol = (u . e2) e2; the mean mode carries nothing. Arithmetic in
+// CT (the field's precision, as the reference computes in its element type).
+template <typename CT>
+__global__ void __launch_bounds__(256) k_toroidal(GridDesc g, KTab kt, const void* u, int f64, void* tor, void* pol,
+                                                  int kept_only) {
+  typedef typename Vec2<CT>::t C2;
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= g.Ntot) return;
+  int k[3];
+  decode_full(g, i, k);
+  if (kept_only && !keep23(g, k)) return;
+  const CT kx = (CT)kt.k[0][k[0]], ky = (CT)kt.k[1][k[1]], kz = (CT)kt.k[2][k[2]];
+  const CT kk = sqrt(kx * kx + ky * ky + kz * kz);
+  const long n = g.Ntot;
+  C2 T[3], Pv[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) T[c] = Pv[c] = mkc<C2>(0, 0);
+  if (kk != (CT)0) {
+    const CT hx = kx / kk, hy = ky / kk, hz = kz / kk;
+    const CT kperp = sqrt(kx * kx + ky * ky);
+    CT e1x = 1, e1y = 0, e1z = 0, e2x = 0, e2y = 1, e2z = 0;
+    if (kperp > (CT)0) {
+      e1x = hy;   // khat x zhat = (hy, -hx, 0)
+      e1y = -hx;
+      e1z = 0;
+      const CT n1 = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+      e1x /= n1;
+      e1y /= n1;
+      e1z /= n1;
+      e2x = hy * e1z - hz * e1y;
+      e2y = hz * e1x - hx * e1z;
+      e2z = hx * e1y - hy * e1x;
+    }
+    const C2 u1 = ld_ct<CT>(u, f64, i), u2 = ld_ct<CT>(u, f64, i + n), u3 = ld_ct<CT>(u, f64, i + 2 * n);
+    const C2 c1 = mkc<C2>(u1.x * e1x + u2.x * e1y + u3.x * e1z, u1.y * e1x + u2.y * e1y + u3.y * e1z);
+    const C2 c2 = mkc<C2>(u1.x * e2x + u2.x * e2y + u3.x * e2z, u1.y * e2x + u2.y * e2y + u3.y * e2z);
+    const CT e1[3] = {e1x, e1y, e1z}, e2[3] = {e2x, e2y, e2z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      T[c] = mkc<C2>(c1.x * e1[c], c1.y * e1[c]);
+      Pv[c] = mkc<C2>(c2.x * e2[c], c2.y * e2[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (f64) {
+      reinterpret_cast<double2*>(tor)[i + n * c] = make_double2((double)T[c].x, (double)T[c].y);
+      reinterpret_cast<double2*>(pol)[i + n * c] = make_double2((double)Pv[c].x, (double)Pv[c].y);
+    } else {
+      reinterpret_cast<float2*>(tor)[i + n * c] = make_float2((float)T[c].x, (float)T[c].y);
+      reinterpret_cast<float2*>(pol)[i + n * c] = make_float2((float)Pv[c].x, (float)Pv[c].y);
+    }
+  }
+}
+
+int toroidal_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* tor, void* pol, cudaStream_t st,
+                   bool kept_only) {
+  if (g.nd != 3) {
+    fit_set_error("ToroidalPoloidalDecomposition is defined in 3D only (got nd=%d).", g.nd);
+    return FIT_ERR_ARG;
+  }
+  if (in_f64) k_toroidal<double><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, tor, pol, kept_only ? 1 : 0);
+  else k_toroidal<float><<<nblk(g.Ntot, 256), 256, 0, st>>>(g, kt, u, in_f64, tor, pol, kept_only ? 1 : 0);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 int helical_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* up, void* um, cudaStream_t st,
                   bool kept_only) {
   if (g.nd != 3) {

@@ -151,6 +151,9 @@ int density_full(const GridDesc& g, const KTab& kt, const void* carrier, const v
 int helical_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* up, void* um,
                   cudaStream_t st,
                   bool kept_only = false);
+// Toroidal / poloidal split of a 3D field (kept_only: only the 2/3-kept modes are touched).
+int toroidal_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* tor, void* pol, cudaStream_t st,
+                   bool kept_only = false);
 // Rotational / divergent (spectral Leray) split of a 2D field.
 int helmholtz_split(const GridDesc& g, const KTab& kt, const void* u, int in_f64, void* rot, void* div,
                     cudaStream_t st);

@@ -61,6 +61,8 @@ static int run_partial(fit_plan* p, PartialState* s, const void* ud, int decompo
   FIT_TRY(pbuf(p, &s->comp, 2 * cb));
   void* comp[2] = {s->comp.p, (char*)s->comp.p + cb};
   if (decomposition == FIT_DECOMP_HELICAL) FIT_TRY(helical_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
+  else if (decomposition == FIT_DECOMP_TOROIDAL_POLOIDAL)
+    FIT_TRY(toroidal_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
   else FIT_TRY(helmholtz_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
   // effective carriers: (invariant j, component sk) -> M fields each
   const size_t csz = sizeof(V) * (size_t)M * g.Mhalf;
@@ -135,6 +137,8 @@ static int run_partial_box(fit_plan* p, PartialState* s, const void* ud, int dec
   void* comp[2] = {s->comp.p, (char*)s->comp.p + cb};
   if (decomposition == FIT_DECOMP_HELICAL) FIT_TRY(helical_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream,
                                                              p->dealias == 1));
+  else if (decomposition == FIT_DECOMP_TOROIDAL_POLOIDAL)
+    FIT_TRY(toroidal_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream, p->dealias == 1));
   else FIT_TRY(helmholtz_split(g, p->kt, ud, p->io_f64, comp[0], comp[1], p->stream));
   FzArgs a;
   fz_box_dims(p, &a);
@@ -307,12 +311,17 @@ extern "C" int fit_partial_fluxes_batched(fit_plan* p, const void* u_hat, int de
     fit_set_error("NULL argument");
     return FIT_ERR_ARG;
   }
-  if (decomposition != FIT_DECOMP_HELICAL && decomposition != FIT_DECOMP_HELMHOLTZ) {
+  if (decomposition != FIT_DECOMP_HELICAL && decomposition != FIT_DECOMP_HELMHOLTZ &&
+      decomposition != FIT_DECOMP_TOROIDAL_POLOIDAL) {
     fit_set_error("calculate_partial_fluxes needs a decomposition that splits u into >=2 named components");
     return FIT_ERR_ARG;
   }
   if (p->M != p->nd || p->Dadv != p->nd) {
     fit_set_error("partial fluxes need an nd-component velocity plan");
+    return FIT_ERR_ARG;
+  }
+  if (decomposition == FIT_DECOMP_TOROIDAL_POLOIDAL && p->nd != 3) {
+    fit_set_error("ToroidalPoloidalDecomposition is defined in 3D only (got nd=%d).", p->nd);
     return FIT_ERR_ARG;
   }
   if (decomposition == FIT_DECOMP_HELICAL && p->nd != 3) {

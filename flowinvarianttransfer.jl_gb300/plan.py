@@ -144,6 +144,14 @@ class Plan:
             check(self.lib.fit_helical_decompose(self.h, self._vp(u), self._vp(up), self._vp(um), PTR_HOST))
         return up, um
 
+    def toroidal_poloidal(self, u_hat):
+        u = self._field(u_hat, self.M)
+        t = np.empty(self.ns + (3,), dtype=self.cdtype, order="F")
+        q = np.empty_like(t)
+        with self.lock:
+            check(self.lib.fit_toroidal_poloidal_decompose(self.h, self._vp(u), self._vp(t), self._vp(q), PTR_HOST))
+        return t, q
+
     def helmholtz(self, u_hat):
         u = self._field(u_hat, self.M)
         r = np.empty(self.ns + (2,), dtype=self.cdtype, order="F")

@@ -128,6 +128,11 @@ class HelmholtzDecomposition(AbstractFieldDecomposition):
     names = ("rotational", "divergent")
 
 
+class ToroidalPoloidalDecomposition(AbstractFieldDecomposition):
+    """Craya-Herring toroidal / poloidal split (``src/Decomposition.jl:107-141``, 3D)."""
+    names = ("toroidal", "poloidal")
+
+
 class RotationalDecomposition(AbstractFieldDecomposition):
     pass
 

@@ -49,6 +49,7 @@ extern "C" {
 /* decompositions (src/Types.jl) */
 #define FIT_DECOMP_HELICAL 1
 #define FIT_DECOMP_HELMHOLTZ 2
+#define FIT_DECOMP_TOROIDAL_POLOIDAL 3  /* src/Decomposition.jl:107-141 (3D) */
 
 /* shell-to-shell execution forms */
 #define FIT_S2S_PLAIN 0    /* one nonlinear term per mediator shell, launched one by one */
@@ -117,6 +118,8 @@ int fit_shell_to_shell(fit_plan* plan, const void* u_hat, const void* adv_hat, c
 int fit_helical_decompose(fit_plan* plan, const void* u_hat, void* u_plus, void* u_minus, int ptr_kind);
 /* Rotational/divergent split of a 2D field (spectral Leray projection; the reference delegates
  * to HelmholtzDecomposition.jl, ext/FlowInvariantTransferHelmholtzDecompositionExt.jl:50-104). */
+/* ToroidalPoloidalDecomposition (src/Decomposition.jl:107-141): u_hat (ns..., 3) -> tor, pol. */
+int fit_toroidal_poloidal_decompose(fit_plan* plan, const void* u_hat, void* tor, void* pol, int ptr_kind);
 int fit_helmholtz_decompose(fit_plan* plan, const void* u_hat, void* u_rot, void* u_div, int ptr_kind);
 
 /* Partial fluxes T^{sk,sp,sq}(k_n) of a two-component decomposition (8 channels). Replaces

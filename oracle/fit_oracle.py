@@ -502,6 +502,8 @@ def partial_fluxes(u_hat, ks, decomposition="helical", binning=None, dealiasing=
         comps = helical_decompose(u_hat, ks)
     elif decomposition == "helmholtz":
         comps = helmholtz_decompose(u_hat, ks)
+    elif decomposition == "toroidal_poloidal":
+        comps = toroidal_poloidal_decompose(u_hat, ks)
     else:
         raise ValueError(decomposition)
     names = list(comps.keys())

@@ -221,3 +221,28 @@ def test_shell_edges_rules():                           # ShellBinning.jl:50-79,
     ks512 = kgrid((512,) * 3)
     kmax = np.sqrt(3) * 256
     assert len(O.shell_edges(("linear", 14.0), kmax)) - 1 == 32
+
+
+def test_toroidal_poloidal_decomposition():    # runtests.jl:634-659
+    M = 8
+    ks = O.wavenumber_grid((M, M, M), (2 * np.pi,) * 3)
+    kx, ky, kz = np.meshgrid(*ks, indexing="ij")
+    rng = np.random.default_rng(52)
+    A = rng.standard_normal((M, M, M, 3)) + 1j * rng.standard_normal((M, M, M, 3))
+    u = np.stack([1j * (ky * A[..., 2] - kz * A[..., 1]), 1j * (kz * A[..., 0] - kx * A[..., 2]),
+                  1j * (kx * A[..., 1] - ky * A[..., 0])], axis=-1)          # solenoidal
+    d = O.toroidal_poloidal_decompose(u, ks)
+    tor, pol = d["toroidal"], d["poloidal"]
+    amax = np.max(np.abs(u))
+    assert np.max(np.abs(tor + pol - u)) <= 1e-12 * amax                      # reconstruction
+    assert abs(np.sum(np.abs(tor) ** 2) + np.sum(np.abs(pol) ** 2) - np.sum(np.abs(u) ** 2)) <= 1e-12 * np.sum(
+        np.abs(u) ** 2)                                                        # orthogonal
+    assert np.max(np.abs(tor[..., 2])) < 1e-12 * amax                         # toroidal: no vertical velocity
+    for f in (tor, pol):
+        assert np.max(np.abs(kx * f[..., 0] + ky * f[..., 1] + kz * f[..., 2])) < 1e-10 * amax   # div-free
+    # the partial fluxes of the split: the eight channels sum to the flux of the whole field
+    u16, ks16 = curl_noise_3d(16, 53)
+    chans, (T, _), _ = O.partial_fluxes(u16, ks16, "toroidal_poloidal", ("linear", 1.0), "two_thirds")
+    _, Tw, _ = O.spectral_flux(u16, ks16, ("linear", 1.0), "two_thirds")
+    assert np.max(np.abs(Tw)) > 1e-6
+    assert np.max(np.abs(T - Tw)) <= 1e-12 * np.max(np.abs(Tw))

@@ -114,3 +114,34 @@ def test_live_box_form_64(deal):
     for name in runs[0]:
         for key, c in runs[0][name].channels.items():
             assert np.array_equal(runs[2][name].channels[key].transfer_spectrum, c.transfer_spectrum)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_toroidal_poloidal_split_and_partial_fluxes(prec):
+    """ToroidalPoloidalDecomposition (src/Decomposition.jl:107-141) on the GPU against the oracle: the
+    split itself, the per-invariant partial fluxes and the one-pass form (eager, replayed)."""
+    u, ks = curl_noise_3d(16, 57)
+    d = F.decompose_field(F.ToroidalPoloidalDecomposition(), u, ks)
+    o = O.toroidal_poloidal_decompose(u, ks)
+    for name in ("toroidal", "poloidal"):
+        assert np.max(np.abs(d[name] - o[name])) <= 1e-12 * np.max(np.abs(o[name]))
+    v = u.astype(np.complex64) if prec == 32 else u
+    r = F.calculate_partial_fluxes(v, ks, decomposition=F.ToroidalPoloidalDecomposition(),
+                                   binning=F.LinearBinning(1.0), spectral=F.GB300Spectral(prec))
+    _check({"KineticEnergy": r}, u, ks, "toroidal_poloidal", "two_thirds", ((F.KineticEnergy(), "ke"),), prec)
+    invs = ((F.KineticEnergy(), "ke"), (F.Helicity(), "helicity"))
+    for _ in range(2):
+        m = F.calculate_partial_fluxes_multi(v, ks, invariants=[i for i, _ in invs],
+                                             decomposition=F.ToroidalPoloidalDecomposition(),
+                                             binning=F.LinearBinning(1.0), spectral=F.GB300Spectral(prec))
+    _check(m, u, ks, "toroidal_poloidal", "two_thirds", invs, prec)
+
+
+def test_toroidal_poloidal_live_box_64():
+    """The toroidal/poloidal split on the live-box partial-flux form (FP32, 64^3)."""
+    u, ks = curl_noise_3d(64, 59)
+    invs = ((F.KineticEnergy(), "ke"), (F.Helicity(), "helicity"))
+    m = F.calculate_partial_fluxes_multi(u, ks, invariants=[i for i, _ in invs],
+                                         decomposition=F.ToroidalPoloidalDecomposition(),
+                                         binning=F.LinearBinning(1.0), spectral=F.GB300Spectral(32))
+    _check(m, u, ks, "toroidal_poloidal", "two_thirds", invs, 32)
