@@ -20,5 +20,6 @@ from .batch import (SpectralFluxBatch, calculate_spectral_flux_batch, autotune_s
 from .closure import (calculate_coarse_graining_flux, evolve_forced_navier_stokes,  # noqa: F401
                       evolve_forced_navier_stokes_device, closure_data, ClosureData, SubfilterStressMLP,
                       gradient_model_flux, field_compare)
+from .replicas import mpi_batch_map, batch_map  # noqa: F401
 from . import _lib  # noqa: F401
 from ._lib import FitError, launch_count, lib_path  # noqa: F401
