@@ -233,7 +233,10 @@ extern "C" int fit_band_to_band(fit_plan* p, const void* u_hat, const void* adv_
   FIT_TRY(ensure(p, &p->outd, sizeof(double) * n_bands * n_bands));
   double* Td = (double*)p->outd.p;
   if (p->prec == 64) FIT_TRY(band_run<double>(p, ud, ad, n_bands, invariant, Td));
-  else FIT_TRY(band_run<float>(p, ud, ad, n_bands, invariant, Td));
+  else if (fz_box_ok(p)) {   // FP32 cubic 3D plans of a fused size: every band through the live-box passes
+    FIT_TRY(s2s_box_bands(p, ud, ad, n_bands, invariant, (const float*)p->wtab.p, Td));
+    FIT_TRY(s2s_check(p));
+  } else FIT_TRY(band_run<float>(p, ud, ad, n_bands, invariant, Td));
   std::vector<double> h((size_t)n_bands * n_bands);
   FIT_CUDA_CHECK(cudaMemcpyAsync(h.data(), Td, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, p->stream));
   FIT_CUDA_CHECK(cudaStreamSynchronize(p->stream));

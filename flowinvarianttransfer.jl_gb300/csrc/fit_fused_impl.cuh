@@ -53,6 +53,10 @@ struct FzArgs {
   // (3 KY P1 complex values each) by velocity uidx[b] of the U array (3 N^3 floats each)
   int hidx[16];
   int uidx[16];
+  // smooth bands: when wbox is set, the z pass multiplies field hidx[b] by the weights of band
+  // widx[b] (box layout [band][kz'][col], KY P1 floats per band) as it loads it
+  const float* wbox;
+  int widx[16];
 };
 
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
@@ -678,7 +682,13 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_bo
         const int f = fz_freq(e, N);
         float2 val = make_float2(0.f, 0.f);
         if (col < a.P1 && f >= -a.K && f <= a.K) {
-          val = Hc[(long)(f + a.K) * a.P1 + col];
+          const long m = (long)(f + a.K) * a.P1 + col;
+          val = Hc[m];
+          if (a.wbox) {
+            const float w = a.wbox[(long)a.widx[b] * a.KY * a.P1 + m];
+            val.x *= w;
+            val.y *= w;
+          }
           if (v) val = fz_muli(val, kd[f + a.K]);
         }
         return val;

@@ -70,6 +70,9 @@ bool fz_box_ok(const fit_plan* p);
 int s2s_box_flux(fit_plan* p, const void* u_dev, const void* a_dev, const void* c_dev, int invariant, double* Tdev);
 // N̂ = FFT[(u . grad) u] through the live-box passes, as the full data-grid spectrum (user layout)
 int s2s_box_nonlinear_full(fit_plan* p, const void* u_dev, void* N_full);
+// smooth band-to-band T(n, m) on the live box (FP32 cubic 3D plans of a fused size; wtab: FP32 weights)
+int s2s_box_bands(fit_plan* p, const void* u_dev, const void* a_dev, int n_bands, int invariant, const float* wtab,
+                  double* Tdev);
 // 1 when the batched shell-to-shell path reads the inputs only on the 2/3-kept box of modes
 int s2s_reads_kept_box(const fit_plan* p);
 void s2s_free(fit_plan* p);

@@ -48,6 +48,10 @@ struct S2SState {
   // fused-path buffers
   fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr, fN;   // fN: the live-box N̂ of the flux form
   int fkd_n = -1;
+  // smooth bands: box layout of the plan's weight table, valid for (fW_key, fW_at)
+  fit_dbuf fW;
+  std::vector<double> fW_key;
+  const void* fW_at = nullptr;
   // per (band shell, pencil tile) lists of the shell's live modes (zinv inputs), rebuilt when the
   // shell table changes
   fit_dbuf zoff, zent, zfill;
@@ -62,7 +66,7 @@ void s2s_free(fit_plan* p) {
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
   fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse,  &s->fsb,  &s->fkd,  &s->fA,
-                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill, &s->fN};
+                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill, &s->fN, &s->fW};
   for (fit_dbuf* b : bufs)
     if (b->p) cudaFree(b->p);
   delete s;
@@ -674,6 +678,190 @@ int s2s_box_nonlinear_full(fit_plan* p, const void* ud, void* Nfull) {
   k_box_to_full<<<(unsigned)((g.Ntot + 255) / 256), 256, 0, p->stream>>>(g, a.K, a.KX, a.KY, a.P1,
                                                                         (const float2*)s->fN.p, Nfull, p->io_f64);
   FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+// Smooth band-to-band transfer on the live box (src/BandTransfer.jl:71-113): the batched mediator
+// pipeline with log-Gaussian weights instead of the shell indicator. H and the carrier are formed
+// once; the box-layout weight table W[n][kz'][col] (taken from the transform grid's half-spectrum
+// table: both conjugate modes of a half mode share |k|) feeds the z pass, which loads w_m H as band
+// m's advected field, and the band binning, which forms
+//     T(n, m) = sum over the box of w_n Re(conj(C) N_m)
+// from the unweighted carrier and every band's nonlinear term in one read of each.
+__global__ void k_box_weight_table(GridDesc g, int K, int KX, int KY, long P1, const float* __restrict__ w, int nb,
+                                   float* __restrict__ W) {
+  const long BL = P1 * KY;
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= BL) return;
+  const long col = i % P1;
+  const int kz = (int)(i / P1), kx = (int)(col % KX), ky = (int)(col / KX);
+  const long hi = kx + (long)g.Mh0 * (fmod_pos(ky - K, g.M[1]) + (long)g.M[1] * fmod_pos(kz - K, g.M[2]));
+  for (int n = 0; n < nb; ++n) W[(long)n * BL + i] = w[(long)n * g.Mhalf + hi];
+}
+
+// Band sums of up to 8 bands x 8 nonlinear terms: per block partial[blk][q * nbat + b] =
+// sum over its modes i with seff(i) != 0 of W[q][i] * sum_c Re(conj(C_c(i)) N_b,c(i)). Each thread
+// sums 32 of its modes in FP32, the warp then reduces those in FP32 and lane 0 adds the result to the
+// warp's own FP64 bins in shared memory (no atomics: the order, hence the result, is fixed); the
+// block sums its warps' bins in warp order.
+__global__ void __launch_bounds__(256) k_box_band_bin(const float2* __restrict__ Nh, long nstride, int nbat,
+                                                      const float2* __restrict__ C, const float* __restrict__ W,
+                                                      int nw, const uint16_t* __restrict__ seff, long BL,
+                                                      double* __restrict__ partial) {
+  __shared__ double bins[8][64];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t = lane; t < 64; t += 32) bins[warp][t] = 0.0;
+  __syncwarp();
+  float part[8][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) part[q][b] = 0.f;
+  const long step = (long)gridDim.x * blockDim.x;
+  // every lane of a warp runs the same number of iterations (warp-uniform trip count), so that the
+  // flushes' shuffles see the whole warp
+  const long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  int cnt = 0;
+  for (long i0 = base; i0 < BL; i0 += step) {
+    const long i = i0 + lane;
+    if (i < BL && seff[i]) {
+      const float2 c0 = C[i], c1 = C[BL + i], c2 = C[2 * BL + i];
+      float d[8];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        d[b] = 0.f;
+        if (b < nbat) {
+          const float2* nb_ = Nh + (long)b * nstride;
+          const float2 x0 = nb_[i], x1 = nb_[BL + i], x2 = nb_[2 * BL + i];
+          d[b] = c0.x * x0.x + c0.y * x0.y + c1.x * x1.x + c1.y * x1.y + c2.x * x2.x + c2.y * x2.y;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nw) {
+          const float w = W[(long)q * BL + i];
+#pragma unroll
+          for (int b = 0; b < 8; ++b)
+            if (b < nbat) part[q][b] += w * d[b];
+        }
+    }
+    const bool last = i0 + step >= BL;
+    if (++cnt == 32 || last) {
+      cnt = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+          if (q < nw && b < nbat) {
+            float v = part[q][b];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) bins[warp][q * 8 + b] += (double)v;
+            part[q][b] = 0.f;
+          }
+    }
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < nw * nbat) {
+    const int q = t / nbat, b = t % nbat;
+    double sum = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += bins[w][q * 8 + b];
+    partial[(long)blockIdx.x * nw * nbat + t] = sum;
+  }
+}
+
+// block partials [blk][q * nbat + b] (fixed order) -> column-major T(n0 + q, m0 + b)
+__global__ void k_box_band_reduce(const double* __restrict__ partial, int nblocks, int nw, int nbat, int n0, int m0,
+                                  int nbands, double* __restrict__ Td) {
+  const int t = threadIdx.x;
+  if (t >= nw * nbat) return;
+  double s = 0.0;
+  for (int k = 0; k < nblocks; ++k) s += partial[(long)k * nw * nbat + t];
+  Td[(long)(m0 + t % nbat) * nbands + n0 + t / nbat] = s;
+}
+
+int s2s_box_bands(fit_plan* p, const void* ud, const void* ad, int nbands, int inv, const float* wtab, double* Td) {
+  S2SState* s = (S2SState*)p->s2s;
+  if (!s) {
+    s = new S2SState();
+    p->s2s = s;
+  }
+  const GridDesc& g = p->g;
+  FzArgs a;
+  fz_box_dims(p, &a);
+  const long BL = (long)a.KY * a.P1;
+  const double M = g.M[0];
+  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
+  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  int B = (int)(40e9 / (8.0 * (perA + perB)));
+  if (B > 16) B = 16;
+  if (B > nbands) B = nbands;
+  if (B < 1) B = 1;
+  FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 6 * BL));   // H, then the advecting field's H
+  FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * BL));
+  FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * BL));
+  FIT_TRY(ensure(p, &s->fsb, sizeof(uint16_t) * BL));
+  FIT_TRY(ensure(p, &s->fkd, sizeof(float) * a.KY));
+  FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA * B)));
+  FIT_TRY(ensure(p, &s->fB, (size_t)(8.0 * perB * B)));
+  FIT_TRY(ensure(p, &s->fN, sizeof(float2) * 3 * BL * B));
+  FIT_TRY(ensure(p, &s->fW, sizeof(float) * BL * nbands));
+  const int nblk = 2 * 152;
+  FIT_TRY(ensure(p, &s->fpart, sizeof(double) * nblk * 64));
+  FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
+  if (!s->ferr.p) {
+    FIT_TRY(ensure(p, &s->ferr, sizeof(int)));
+    FIT_CUDA_CHECK(cudaMemset(s->ferr.p, 0, sizeof(int)));
+  }
+  if (s->fkd_n != a.KY) {
+    FIT_TRY(fz_box_kd(p, a, (float*)s->fkd.p));
+    s->fkd_n = a.KY;
+  }
+  float* W = (float*)s->fW.p;
+  if (s->fW_key != p->wtab_key || s->fW_at != s->fW.p) {   // box layout of the plan's current weight table
+    k_box_weight_table<<<(unsigned)((BL + 255) / 256), 256, 0, p->stream>>>(g, a.K, a.KX, a.KY, a.P1, wtab, nbands,
+                                                                           W);
+    FIT_LAUNCH_CHECK();
+    s->fW_key = p->wtab_key;
+    s->fW_at = s->fW.p;
+  }
+  float2* H = (float2*)s->fH.p;
+  float2* C = (float2*)s->fC.p;
+  uint16_t* se = (uint16_t*)s->fse.p;
+  uint16_t* sb = (uint16_t*)s->fsb.p;
+  const float2* Hadv = H;
+  if (ad != ud) {   // advecting field first (its carrier and shell maps are scratch, rewritten by u's)
+    FIT_TRY(fz_box_setup(p, a, ad, inv, H + 3 * BL, (float2*)s->fN.p, se, sb, -1, nullptr));
+    Hadv = H + 3 * BL;
+  }
+  FIT_TRY(fz_box_setup(p, a, ud, inv, H, C, se, sb, -1, nullptr));
+  FIT_TRY(fz_box_velocity(p, a, Hadv, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p));
+  double* part = (double*)s->fpart.p;
+  a.wbox = W;
+  for (int m0 = 0; m0 < nbands; m0 += B) {
+    a.nb = nbands - m0 < B ? nbands - m0 : B;
+    for (int b = 0; b < a.nb; ++b) {
+      a.hidx[b] = 0;
+      a.uidx[b] = 0;
+      a.widx[b] = m0 + b;
+      a.ext[b][0] = a.ext[b][1] = a.ext[b][2] = (short)a.K;
+    }
+    FIT_TRY(fz_box_terms(p, a, H, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
+                         (float2*)s->fB.p, (float2*)s->fN.p, (int*)s->ferr.p));
+    for (int b0 = 0; b0 < a.nb; b0 += 8) {
+      const int nbat = a.nb - b0 < 8 ? a.nb - b0 : 8;
+      for (int n0 = 0; n0 < nbands; n0 += 8) {
+        const int nw = nbands - n0 < 8 ? nbands - n0 : 8;
+        fit_prof_begin(PK_BIN, (double)BL * (24.0 * (nbat + 1) + 4.0 * nw + 2.0), p->stream);
+        k_box_band_bin<<<nblk, 256, 0, p->stream>>>((const float2*)s->fN.p + (long)b0 * 3 * BL, 3 * BL, nbat, C,
+                                                    W + (long)n0 * BL, nw, se, BL, part);
+        fit_prof_end(p->stream);
+        FIT_LAUNCH_CHECK();
+        k_box_band_reduce<<<1, 64, 0, p->stream>>>(part, nblk, nw, nbat, n0, m0 + b0, nbands, Td);
+        FIT_LAUNCH_CHECK();
+      }
+    }
+  }
   return FIT_OK;
 }
 

@@ -247,6 +247,14 @@ class Plan:
                                           C.c_void_p(asym_ptr) if asym_ptr else None, PTR_DEVICE))
 
 
+    def band_to_band_device(self, u_ptr, a_ptr, centers, logwidth, dmask, coord_f32, inv, T_ptr, net_ptr,
+                            asym_ptr):
+        c = np.ascontiguousarray(centers, dtype=np.float64)
+        check(self.lib.fit_band_to_band(self.h, C.c_void_p(u_ptr), C.c_void_p(a_ptr) if a_ptr else None, _dptr(c),
+                                        len(c), float(logwidth), dmask, int(coord_f32), inv, C.c_void_p(T_ptr),
+                                        C.c_void_p(net_ptr) if net_ptr else None,
+                                        C.c_void_p(asym_ptr) if asym_ptr else None, PTR_DEVICE))
+
     def mode_to_mode_device(self, u_ptr, inv, fp64, S_ptr, net_ptr):
         check(self.lib.fit_mode_to_mode(self.h, C.c_void_p(u_ptr), None, inv, int(fp64), C.c_void_p(S_ptr),
                                         C.c_void_p(net_ptr), PTR_DEVICE))

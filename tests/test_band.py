@@ -66,3 +66,43 @@ def test_band_scalar():
                                           advecting_hat=u, spectral=F.GB300Spectral(64))
     _, T, _, _ = O.band_to_band(th, ks, [1.0, 2.5, 5.0], 0.5, "two_thirds", "scalar", adv_hat=u)
     assert np.max(np.abs(r.transfer_matrix - T)) <= 1e-11 * np.sqrt(np.sum(T ** 2))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deal,inv,adv", [("two_thirds", "ke", False), ("three_halves", "ke", False),
+                                          ("two_thirds", "helicity", False), ("two_thirds", "ke", True)])
+def test_band_3d_live_box_fp32(deal, inv, adv):
+    """FP32 cubic 64^3 fields take the live-box form (weighted band copies through the fused passes,
+    weighted carriers binned in one pass); same matrix as the oracle within FP32 accuracy."""
+    u, ks = curl_noise_3d(64, 11)
+    a = curl_noise_3d(64, 12)[0] if adv else None
+    DEAL = {"two_thirds": F.OrszagTwoThirds(), "three_halves": F.PaddedThreeHalves()}
+    INV = {"ke": F.KineticEnergy(), "helicity": F.Helicity()}
+    centers = [2.0, 4.0, 8.0, 16.0]
+    r = F.calculate_band_to_band_transfer(u.astype(np.complex64), ks, F.SmoothBands(centers, 0.5),
+                                          dealiasing=DEAL[deal], invariant=INV[inv], spectral=F.GB300Spectral(32),
+                                          advecting_hat=None if a is None else a.astype(np.complex64))
+    _, T, net, asym = O.band_to_band(u, ks, centers, 0.5, deal, inv, adv_hat=a)
+    Tn = np.sqrt(np.sum(T ** 2))
+    assert Tn > 0
+    assert np.max(np.abs(r.transfer_matrix - T)) <= 2e-5 * Tn, (deal, inv, adv)
+    assert np.max(np.abs(r.net_transfer - net)) <= 2e-5 * Tn
+    # kinetic energy self-advected under the 2/3 rule is antisymmetric up to FP32 rounding; helicity
+    # band pairs are not, nor is the 3/2 rule on this white-noise field (its Nyquist modes), nor
+    # advection by another field: there the oracle's own value is the reference
+    assert abs(r.max_antisymmetry_error - asym) <= 5e-5 * Tn
+    if not adv and deal == "two_thirds" and inv == "ke":
+        assert r.max_antisymmetry_error <= 2e-5 * Tn
+
+
+@pytest.mark.gpu
+def test_band_live_box_many_bands_match_plain_path():
+    """12 bands (two binning passes of at most 8 carrier sets each) on the live box against the
+    plan's FP64 path on the same 64^3 field."""
+    u, ks = curl_noise_3d(64, 5)
+    centers = list(np.geomspace(1.0, 24.0, 12))
+    r32 = F.calculate_band_to_band_transfer(u.astype(np.complex64), ks, F.SmoothBands(centers, 0.4),
+                                            spectral=F.GB300Spectral(32))
+    r64 = F.calculate_band_to_band_transfer(u, ks, F.SmoothBands(centers, 0.4), spectral=F.GB300Spectral(64))
+    Tn = np.sqrt(np.sum(r64.transfer_matrix ** 2))
+    assert np.max(np.abs(r32.transfer_matrix - r64.transfer_matrix)) <= 2e-5 * Tn
