@@ -1056,26 +1056,29 @@ def run_band(args):
     del plan
     F.clear_plans()
     torch.cuda.empty_cache()
-    # the plain per-band path in FP32 (live box switched off for this plan)
-    os.environ["FIT_NO_FUSED"] = "1"
-    try:
-        pp = F.Plan(ns, 3, 3, "two_thirds", 32, False, ks)
-        pp.set_stream(stream.cuda_stream)
-        Tp = torch.zeros((nb, nb), dtype=torch.float64, device=dev)
-        ms_plain32 = _timed_ms(lambda: run(pp, u, Tp), stream, 1, warm=1)
-        del pp
-    finally:
-        del os.environ["FIT_NO_FUSED"]
-    F.clear_plans()
-    torch.cuda.empty_cache()
-    u64 = u.to(torch.complex128)
-    p64 = F.Plan(ns, 3, 3, "two_thirds", 64, True, ks)
-    p64.set_stream(stream.cuda_stream)
-    T64 = torch.zeros((nb, nb), dtype=torch.float64, device=dev)
-    ms64 = _timed_ms(lambda: run(p64, u64, T64), stream, 1, warm=1)
-    T64n = T64.cpu().numpy().T.copy()
-    del p64, u64
-    F.clear_plans()
+    ms_plain32 = ms64 = None
+    T64n = T32
+    if not args.no_fp64:
+        # the plain per-band path in FP32 (live box switched off for this plan)
+        os.environ["FIT_NO_FUSED"] = "1"
+        try:
+            pp = F.Plan(ns, 3, 3, "two_thirds", 32, False, ks)
+            pp.set_stream(stream.cuda_stream)
+            Tp = torch.zeros((nb, nb), dtype=torch.float64, device=dev)
+            ms_plain32 = _timed_ms(lambda: run(pp, u, Tp), stream, 1, warm=1)
+            del pp
+        finally:
+            del os.environ["FIT_NO_FUSED"]
+        F.clear_plans()
+        torch.cuda.empty_cache()
+        u64 = u.to(torch.complex128)
+        p64 = F.Plan(ns, 3, 3, "two_thirds", 64, True, ks)
+        p64.set_stream(stream.cuda_stream)
+        T64 = torch.zeros((nb, nb), dtype=torch.float64, device=dev)
+        ms64 = _timed_ms(lambda: run(p64, u64, T64), stream, 1, warm=1)
+        T64n = T64.cpu().numpy().T.copy()
+        del p64, u64
+        F.clear_plans()
     scale = float(np.max(np.abs(T64n)))
     line = {"metric": f"{N}^3 smooth band-to-band T(K,Q), {nb} bands: matrices/s", "value": 1000.0 / ms,
             "unit": "matrices/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
@@ -1085,9 +1088,10 @@ def run_band(args):
                                    "complex64 field, FP64 sums",
                        "spectrum": "k^-5/3 on [4,170], k^4 rise below 4, solenoidal", "seed": args.seed,
                        "l2": "field 3.2 GB per step >> 129 MB L2"},
-            "roofline": roofline, "ms_plain_fp32": ms_plain32, "speedup_vs_plain_fp32": ms_plain32 / ms,
-            "ms_plain_fp64": ms64, "speedup_vs_plain_fp64": ms64 / ms,
-            "rel_err_vs_fp64_maxnorm": float(np.max(np.abs(T32 - T64n)) / scale),
+            "roofline": roofline, "ms_plain_fp32": ms_plain32,
+            "speedup_vs_plain_fp32": None if ms_plain32 is None else ms_plain32 / ms,
+            "ms_plain_fp64": ms64, "speedup_vs_plain_fp64": None if ms64 is None else ms64 / ms,
+            "rel_err_vs_fp64_maxnorm": None if ms64 is None else float(np.max(np.abs(T32 - T64n)) / scale),
             "antisymmetry_fp32_rel": asym32 / scale,
             "conservation_fp32": float(abs(T32.sum()) / np.abs(T32).sum()),
             "gpu_launches": int(launches), "clocks": clocks}

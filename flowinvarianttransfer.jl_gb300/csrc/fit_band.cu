@@ -38,20 +38,16 @@ FIT_D double band_kappa(const GridDesc& g, const KTab& kt, unsigned dims, int f3
   return __dsqrt_rn(s);
 }
 
-// w[n][i] for every half mode i of the transform grid (zero when no N-grid mode maps to it).
-template <typename S>
-__global__ void k_band_weights(GridDesc g, KTab kt, unsigned dims, int f32, const double* __restrict__ centers,
-                               int nb, double logwidth, S* __restrict__ w) {
-  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= g.Mhalf) return;
-  int g0, g1, g2;
-  decode_half(g, i, &g0, &g1, &g2);
+// Normalised weights of transform-grid half mode (g0, g1, g2) (zero when no N-grid mode maps to it):
+// w_n = exp(-ln(kappa / c_n)^2 / (2 logwidth^2)) / sum over bands, 0 at kappa = 0
+// (src/BandTransfer.jl:24-48).
+FIT_D void band_weights_at(const GridDesc& g, const KTab& kt, unsigned dims, int f32, const double* centers, int nb,
+                           double logwidth, int g0, int g1, int g2, double* wn) {
   KIdx kA, kB;
   map_pair(g, g0, g1, g2, &kA, &kB);
   const KIdx& k = kA.lin >= 0 ? kA : kB;
   double kappa = 0.0;
   if (k.lin >= 0) kappa = band_kappa(g, kt, dims, f32, k.k);
-  double wn[16];
   double sum = 0.0;
 #pragma unroll
   for (int n = 0; n < 16; ++n) {
@@ -63,8 +59,39 @@ __global__ void k_band_weights(GridDesc g, KTab kt, unsigned dims, int f32, cons
     }
   }
 #pragma unroll
+  for (int n = 0; n < 16; ++n) wn[n] = sum > 0.0 ? wn[n] / sum : 0.0;
+}
+
+// w[n][i] for every half mode i of the transform grid.
+template <typename S>
+__global__ void k_band_weights(GridDesc g, KTab kt, unsigned dims, int f32, const double* __restrict__ centers,
+                               int nb, double logwidth, S* __restrict__ w) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= g.Mhalf) return;
+  int g0, g1, g2;
+  decode_half(g, i, &g0, &g1, &g2);
+  double wn[16];
+  band_weights_at(g, kt, dims, f32, centers, nb, logwidth, g0, g1, g2, wn);
+#pragma unroll
   for (int n = 0; n < 16; ++n)
-    if (n < nb) w[(long)n * g.Mhalf + i] = (S)(sum > 0.0 ? wn[n] / sum : 0.0);
+    if (n < nb) w[(long)n * g.Mhalf + i] = (S)wn[n];
+}
+
+// The same weights on the live box of the fused FP32 path only, layout [n][kz'][kx + KX ky'] (box mode
+// (kx, ky' - K, kz' - K)): a quarter of the half spectrum at 512^3 with the 2/3 rule.
+__global__ void k_band_weights_box(GridDesc g, KTab kt, int K, int KX, int KY, unsigned dims, int f32,
+                                   const double* __restrict__ centers, int nb, double logwidth, float* __restrict__ w) {
+  const long P1 = (long)KX * KY, BL = P1 * KY;
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= BL) return;
+  const long col = i % P1;
+  const int kz = (int)(i / P1), kx = (int)(col % KX), ky = (int)(col / KX);
+  double wn[16];
+  band_weights_at(g, kt, dims, f32, centers, nb, logwidth, kx, fmod_pos(ky - K, g.M[1]), fmod_pos(kz - K, g.M[2]),
+                  wn);
+#pragma unroll
+  for (int n = 0; n < 16; ++n)
+    if (n < nb) w[(long)n * BL + i] = (float)wn[n];
 }
 
 // out[n] = sum over half modes i with seff(i) != 0 of w[n][i] * sum_c Re(conj(ceff_c(i)) nh_c(i)).
@@ -208,20 +235,30 @@ extern "C" int fit_band_to_band(fit_plan* p, const void* u_hat, const void* adv_
   // 2/3-discarded modes)
   const double all[2] = {0.0, 1e300};
   FIT_TRY(ensure_shells(p, all, 2, dims_mask, coord_f32));
-  // weight table, cached per (centers, logwidth, dims, coordinate type)
+  // weight table, cached per (centers, logwidth, dims, coordinate type, layout): on the live box for
+  // FP32 cubic 3D plans of a fused size, else on the transform grid's half spectrum
+  const bool box = p->prec == 32 && fz_box_ok(p);
+  int bK = 0, bKX = 0, bKY = 0;
+  long bP1 = 0;
+  if (box) fz_box_geom(p, &bK, &bKX, &bKY, &bP1);
+  const long nw = box ? bP1 * bKY : p->g.Mhalf;
   std::vector<double> key(centers, centers + n_bands);
   key.push_back(logwidth);
   key.push_back((double)dims_mask);
   key.push_back((double)coord_f32);
   key.push_back((double)p->prec);
+  key.push_back((double)box);
   if (key != p->wtab_key) {
-    const size_t wb = ((p->prec == 64 ? 8 : 4) * (size_t)n_bands * p->g.Mhalf + 255) / 256 * 256;
+    const size_t wb = ((p->prec == 64 ? 8 : 4) * (size_t)n_bands * nw + 255) / 256 * 256;
     FIT_TRY(ensure(p, &p->wtab, wb + sizeof(double) * n_bands));
     double* cdev = (double*)((char*)p->wtab.p + wb);   // band centres after the table
     FIT_CUDA_CHECK(cudaMemcpyAsync(cdev, centers, sizeof(double) * n_bands, cudaMemcpyHostToDevice, p->stream));
     const unsigned dm = dims_mask ? dims_mask : ((1u << p->nd) - 1u);
-    const unsigned nblk = (unsigned)((p->g.Mhalf + 255) / 256);
-    if (p->prec == 64)
+    const unsigned nblk = (unsigned)((nw + 255) / 256);
+    if (box)
+      k_band_weights_box<<<nblk, 256, 0, p->stream>>>(p->g, p->kt, bK, bKX, bKY, dm, coord_f32, cdev, n_bands,
+                                                      logwidth, (float*)p->wtab.p);
+    else if (p->prec == 64)
       k_band_weights<double><<<nblk, 256, 0, p->stream>>>(p->g, p->kt, dm, coord_f32, cdev, n_bands, logwidth,
                                                           (double*)p->wtab.p);
     else
@@ -233,7 +270,7 @@ extern "C" int fit_band_to_band(fit_plan* p, const void* u_hat, const void* adv_
   FIT_TRY(ensure(p, &p->outd, sizeof(double) * n_bands * n_bands));
   double* Td = (double*)p->outd.p;
   if (p->prec == 64) FIT_TRY(band_run<double>(p, ud, ad, n_bands, invariant, Td));
-  else if (fz_box_ok(p)) {   // FP32 cubic 3D plans of a fused size: every band through the live-box passes
+  else if (box) {   // FP32 cubic 3D plans of a fused size: every band through the live-box passes
     FIT_TRY(s2s_box_bands(p, ud, ad, n_bands, invariant, (const float*)p->wtab.p, Td));
     FIT_TRY(s2s_check(p));
   } else FIT_TRY(band_run<float>(p, ud, ad, n_bands, invariant, Td));

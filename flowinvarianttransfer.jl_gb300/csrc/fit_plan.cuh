@@ -70,8 +70,11 @@ bool fz_box_ok(const fit_plan* p);
 int s2s_box_flux(fit_plan* p, const void* u_dev, const void* a_dev, const void* c_dev, int invariant, double* Tdev);
 // N̂ = FFT[(u . grad) u] through the live-box passes, as the full data-grid spectrum (user layout)
 int s2s_box_nonlinear_full(fit_plan* p, const void* u_dev, void* N_full);
-// smooth band-to-band T(n, m) on the live box (FP32 cubic 3D plans of a fused size; wtab: FP32 weights)
-int s2s_box_bands(fit_plan* p, const void* u_dev, const void* a_dev, int n_bands, int invariant, const float* wtab,
+// the live box of the fused path: modes (kx, ky' - K, kz' - K), 0 <= kx < KX, 0 <= ky', kz' < KY, P1 = KX KY
+void fz_box_geom(const fit_plan* p, int* K, int* KX, int* KY, long* P1);
+// smooth band-to-band T(n, m) on the live box (FP32 cubic 3D plans of a fused size); W: FP32 band
+// weights in box layout [band][kz'][kx + KX ky']
+int s2s_box_bands(fit_plan* p, const void* u_dev, const void* a_dev, int n_bands, int invariant, const float* W,
                   double* Tdev);
 // 1 when the batched shell-to-shell path reads the inputs only on the 2/3-kept box of modes
 int s2s_reads_kept_box(const fit_plan* p);

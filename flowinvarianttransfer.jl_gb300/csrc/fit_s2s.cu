@@ -48,10 +48,6 @@ struct S2SState {
   // fused-path buffers
   fit_dbuf fH, fC, fse, fsb, fkd, fA, fB, fpart, ferr, fN;   // fN: the live-box N̂ of the flux form
   int fkd_n = -1;
-  // smooth bands: box layout of the plan's weight table, valid for (fW_key, fW_at)
-  fit_dbuf fW;
-  std::vector<double> fW_key;
-  const void* fW_at = nullptr;
   // per (band shell, pencil tile) lists of the shell's live modes (zinv inputs), rebuilt when the
   // shell table changes
   fit_dbuf zoff, zent, zfill;
@@ -66,7 +62,7 @@ void s2s_free(fit_plan* p) {
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
   fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse,  &s->fsb,  &s->fkd,  &s->fA,
-                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill, &s->fN, &s->fW};
+                      &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill, &s->fN};
   for (fit_dbuf* b : bufs)
     if (b->p) cudaFree(b->p);
   delete s;
@@ -683,21 +679,10 @@ int s2s_box_nonlinear_full(fit_plan* p, const void* ud, void* Nfull) {
 
 // Smooth band-to-band transfer on the live box (src/BandTransfer.jl:71-113): the batched mediator
 // pipeline with log-Gaussian weights instead of the shell indicator. H and the carrier are formed
-// once; the box-layout weight table W[n][kz'][col] (taken from the transform grid's half-spectrum
-// table: both conjugate modes of a half mode share |k|) feeds the z pass, which loads w_m H as band
-// m's advected field, and the band binning, which forms
+// once; the box-layout weight table W[n][kz'][col] (both conjugate modes of a half mode share |k|)
+// feeds the z pass, which loads w_m H as band m's advected field, and the band binning, which forms
 //     T(n, m) = sum over the box of w_n Re(conj(C) N_m)
 // from the unweighted carrier and every band's nonlinear term in one read of each.
-__global__ void k_box_weight_table(GridDesc g, int K, int KX, int KY, long P1, const float* __restrict__ w, int nb,
-                                   float* __restrict__ W) {
-  const long BL = P1 * KY;
-  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= BL) return;
-  const long col = i % P1;
-  const int kz = (int)(i / P1), kx = (int)(col % KX), ky = (int)(col / KX);
-  const long hi = kx + (long)g.Mh0 * (fmod_pos(ky - K, g.M[1]) + (long)g.M[1] * fmod_pos(kz - K, g.M[2]));
-  for (int n = 0; n < nb; ++n) W[(long)n * BL + i] = w[(long)n * g.Mhalf + hi];
-}
 
 // Band sums of up to 8 bands x 8 nonlinear terms: per block partial[blk][q * nbat + b] =
 // sum over its modes i with seff(i) != 0 of W[q][i] * sum_c Re(conj(C_c(i)) N_b,c(i)). Each thread
@@ -780,7 +765,16 @@ __global__ void k_box_band_reduce(const double* __restrict__ partial, int nblock
   Td[(long)(m0 + t % nbat) * nbands + n0 + t / nbat] = s;
 }
 
-int s2s_box_bands(fit_plan* p, const void* ud, const void* ad, int nbands, int inv, const float* wtab, double* Td) {
+void fz_box_geom(const fit_plan* p, int* K, int* KX, int* KY, long* P1) {
+  FzArgs a;
+  fz_box_dims(p, &a);
+  *K = a.K;
+  *KX = a.KX;
+  *KY = a.KY;
+  *P1 = a.P1;
+}
+
+int s2s_box_bands(fit_plan* p, const void* ud, const void* ad, int nbands, int inv, const float* W, double* Td) {
   S2SState* s = (S2SState*)p->s2s;
   if (!s) {
     s = new S2SState();
@@ -805,7 +799,6 @@ int s2s_box_bands(fit_plan* p, const void* ud, const void* ad, int nbands, int i
   FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA * B)));
   FIT_TRY(ensure(p, &s->fB, (size_t)(8.0 * perB * B)));
   FIT_TRY(ensure(p, &s->fN, sizeof(float2) * 3 * BL * B));
-  FIT_TRY(ensure(p, &s->fW, sizeof(float) * BL * nbands));
   const int nblk = 2 * 152;
   FIT_TRY(ensure(p, &s->fpart, sizeof(double) * nblk * 64));
   FIT_TRY(ensure(p, &p->ph, sizeof(float) * 3 * g.Mtot));
@@ -816,14 +809,6 @@ int s2s_box_bands(fit_plan* p, const void* ud, const void* ad, int nbands, int i
   if (s->fkd_n != a.KY) {
     FIT_TRY(fz_box_kd(p, a, (float*)s->fkd.p));
     s->fkd_n = a.KY;
-  }
-  float* W = (float*)s->fW.p;
-  if (s->fW_key != p->wtab_key || s->fW_at != s->fW.p) {   // box layout of the plan's current weight table
-    k_box_weight_table<<<(unsigned)((BL + 255) / 256), 256, 0, p->stream>>>(g, a.K, a.KX, a.KY, a.P1, wtab, nbands,
-                                                                           W);
-    FIT_LAUNCH_CHECK();
-    s->fW_key = p->wtab_key;
-    s->fW_at = s->fW.p;
   }
   float2* H = (float2*)s->fH.p;
   float2* C = (float2*)s->fC.p;
