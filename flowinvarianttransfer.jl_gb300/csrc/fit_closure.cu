@@ -172,8 +172,14 @@ static int forward_spectrum(fit_plan* p, const void* u_dev, void* out_dev) {
   const GridDesc& g = p->g;
   const int nf = p->M;
   const long n = g.Mtot;
-  FIT_TRY(ensure(p, &p->ph, sizeof(T) * nf * n));
   FIT_TRY(ensure(p, &p->nh, sizeof(V) * nf * g.Mhalf));
+  const bool same = (p->io_f64 != 0) == (sizeof(T) == 8);
+  if (same) {   // the real fields are read in place; the z pass writes the full spectrum itself
+    const int rc = forward_nd_full<T>((const T*)u_dev, (V*)p->nh.p, (V*)out_dev, g, p->ax, nf,
+                                      (T)(1.0 / (double)n), p->stream);
+    if (rc != 1) return rc;
+  }
+  FIT_TRY(ensure(p, &p->ph, sizeof(T) * nf * n));
   T* ph = (T*)p->ph.p;
   if (p->io_f64 && sizeof(T) == 4) {
     k_convert_real<double, T><<<cl_blk(nf * n, 256), 256, 0, p->stream>>>((const double*)u_dev, ph, nf * n);

@@ -46,6 +46,20 @@ static int ct_strided_n(const V* in, V* out, long P, long Q, typename Scal<V>::t
 }
 
 template <typename V, int N>
+static int ct_z_full_n(const V* in, V* out, int N0, int Mh0, int N1, long Q, const V* tw, cudaStream_t st) {
+  typedef CtTile<V, N> TT;
+  const long tpq = ((long)Mh0 * N1 + TT::C - 1) / TT::C;
+  const long grid = tpq * Q;
+  if (grid > 2147483647L) {
+    fit_set_error("grid too large");
+    return FIT_ERR_SIZE;
+  }
+  FIT_TRY(ct_prep(k_ct_z_full<V, N>, TT::SMEM, TT::NTHR));
+  k_ct_z_full<V, N><<<(unsigned)grid, TT::NTHR, TT::SMEM, st>>>(in, out, N0, Mh0, N1, tpq, tw);
+  return FIT_OK;
+}
+
+template <typename V, int N>
 static int ct_c2r_n(const V* in, typename Scal<V>::t* out, long L, typename Scal<V>::t scale, const V* tw,
                     cudaStream_t st) {
   typedef CtTile<V, N> TT;
@@ -75,6 +89,20 @@ int ct_strided(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, int N, l
     return inv ? ct_strided_n<V, true, n>(in, out, P, Q, scale, tw, st)             \
                : ct_strided_n<V, false, n>(in, out, P, Q, scale, tw, st);
   switch (N) {
+    FIT_CT_SIZES(FIT_CT_CASE)
+    default: return 1;
+  }
+#undef FIT_CT_CASE
+}
+
+// Returns 1 when the z length has no compile-time kernel.
+template <typename T>
+int ct_z_full(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, int N0, int Mh0, int N1, int N2, long Q,
+              const typename Vec2<T>::t* tw, cudaStream_t st) {
+  typedef typename Vec2<T>::t V;
+#define FIT_CT_CASE(n) \
+  case n: return ct_z_full_n<V, n>(in, out, N0, Mh0, N1, Q, tw, st);
+  switch (N2) {
     FIT_CT_SIZES(FIT_CT_CASE)
     default: return 1;
   }

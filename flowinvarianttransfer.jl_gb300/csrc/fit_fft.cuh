@@ -428,6 +428,55 @@ __global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_strided(const V* in, 
   }
 }
 
+// Forward z pass of an unpadded 3D half spectrum (columns kx + Mh0 ky of each of the nf fields,
+// z stride Mh0 N1) whose store writes the full N-grid spectrum (x fastest, field slowest): mode
+// (kx, ky, kz) and, for 0 < kx < N0/2, its conjugate mirror (N0 - kx, -ky, -kz), so that no separate
+// scatter pass reads the half spectrum again.
+template <typename V, int N>
+__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_z_full(const V* __restrict__ in, V* __restrict__ out,
+                                                                 int N0, int Mh0, int N1, long tilesPerQ,
+                                                                 const V* __restrict__ twg) {
+  typedef CtTile<V, N> TT;
+  constexpr int C = TT::C, E = TT::E;
+  extern __shared__ __align__(16) unsigned char fit_smem_raw[];
+  V* s = reinterpret_cast<V*>(fit_smem_raw);
+  V* tw = s + E;
+  const int tid = threadIdx.x;
+  const long tile = blockIdx.x;
+  const long q = tile / tilesPerQ;
+  const long P = (long)Mh0 * N1;
+  const long c0 = (tile - q * tilesPerQ) * C;
+  const long base = q * P * (long)N;
+  const long plane = (long)N0 * N1, obase = q * plane * N;
+  for (int t = tid; t < N; t += TT::NTHR) tw[t] = twg[t];
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i % C, e = i / C;
+    const long col = c0 + c;
+    V x = mkc<V>(0, 0);
+    if (col < P) x = in[base + col + (long)e * P];
+    s[swz(e, c, C)] = x;
+  }
+  __syncthreads();
+  ct_stages<V, false, N, C, TT::NTHR, TT::EPT, 0>(s, tw, tid);
+#pragma unroll 4
+  for (int i = tid; i < E; i += TT::NTHR) {
+    const int c = i % C, kz = i / C;
+    const long col = c0 + c;
+    if (col < P) {
+      const int kx = (int)(col % Mh0), ky = (int)(col / Mh0);
+      const V v = s[swz(kz, c, C)];
+      out[obase + kx + (long)N0 * ky + plane * kz] = v;
+      if (kx > 0 && 2 * kx < N0) {
+        V m = v;
+        m.y = -m.y;
+        const int my = ky == 0 ? 0 : N1 - ky, mz = kz == 0 ? 0 : N - kz;
+        out[obase + (N0 - kx) + (long)N0 * my + plane * mz] = m;
+      }
+    }
+  }
+}
+
 template <typename V, int N>
 __global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_c2r_x(const V* __restrict__ in,
                                                                 typename Scal<V>::t* __restrict__ out, long L,

@@ -40,6 +40,12 @@ int inverse_nd(typename Vec2<T>::t* half, T* phys, const GridDesc& g, const Axis
 template <typename T>
 int forward_nd(const T* phys, typename Vec2<T>::t* half, const GridDesc& g, const Axis* ax, long nf, T scale,
                cudaStream_t st);
+// forward_nd straight into the full N-grid spectrum (x fastest, field slowest) of unpadded 3D grids:
+// the z pass stores every mode and its conjugate mirror. Returns 1 (nothing launched) when the grid
+// is not an unpadded 3D grid or its z length has no compile-time kernel.
+template <typename T>
+int forward_nd_full(const T* phys, typename Vec2<T>::t* half, typename Vec2<T>::t* full, const GridDesc& g,
+                    const Axis* ax, long nf, T scale, cudaStream_t st);
 
 // Pass autotuner (fit_passes.cu): on/off, reset, summary and per-entry readout.
 void autotune_enable(bool on);

@@ -23,6 +23,9 @@ int ct_c2r(const typename Vec2<T>::t* in, T* out, int N, long L, T scale, const 
 template <typename T>
 int ct_r2c(const T* in, typename Vec2<T>::t* out, int N, long L, T scale, const typename Vec2<T>::t* tw,
            cudaStream_t st);
+template <typename T>
+int ct_z_full(const typename Vec2<T>::t* in, typename Vec2<T>::t* out, int N0, int Mh0, int N1, int N2, long Q,
+              const typename Vec2<T>::t* tw, cudaStream_t st);
 
 int axis_init(Axis* a, int N) {
   a->N = N;
@@ -561,6 +564,29 @@ int forward_nd(const T* phys, typename Vec2<T>::t* half, const GridDesc& g, cons
   return FIT_OK;
 }
 
+template <typename T>
+int forward_nd_full(const T* phys, typename Vec2<T>::t* half, typename Vec2<T>::t* full, const GridDesc& g,
+                    const Axis* ax, long nf, T scale, cudaStream_t st) {
+  if (g.nd != 3 || g.padded) return 1;
+  const int n2 = g.M[2];
+  bool ct = false;
+  for (int n : {8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024}) ct = ct || n == n2;
+  if (!ct) return 1;
+  const long Mh0 = g.Mh0, M1 = g.M[1], M2 = g.M[2];
+  FIT_TRY(pass_r2c_x<T>(phys, half, ax[0], M1 * M2 * nf, scale, st));
+  FIT_TRY(pass_strided<T>(half, half, ax[1], Mh0, M2 * nf, false, (T)1, st));
+  fit_prof_begin(PK_FFT_STRIDED, (double)nf * Mh0 * M1 * M2 * sizeof(typename Vec2<T>::t) * 3.0, st);
+  const int rc = ct_z_full<T>(half, full, g.M[0], (int)Mh0, (int)M1, n2, nf, axis_tw<T>(ax[2]), st);
+  fit_prof_end(st);
+  if (rc != FIT_OK) return rc == 1 ? FIT_ERR_SIZE : rc;
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
+template int forward_nd_full<float>(const float*, float2*, float2*, const GridDesc&, const Axis*, long, float,
+                                    cudaStream_t);
+template int forward_nd_full<double>(const double*, double2*, double2*, const GridDesc&, const Axis*, long, double,
+                                     cudaStream_t);
 template int pass_strided<float>(const float2*, float2*, const Axis&, long, long, bool, float, cudaStream_t);
 template int pass_strided<double>(const double2*, double2*, const Axis&, long, long, bool, double, cudaStream_t);
 template int pass_c2r_x<float>(const float2*, float*, const Axis&, long, float, cudaStream_t);

@@ -125,14 +125,18 @@ FILTERS = {"sharp": F.SharpSpectralFilter(), "gaussian": F.GaussianFilter(), "to
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", [64, 32])
-def test_forward_spectrum(prec):
-    ns = (24, 16, 8)
+@pytest.mark.parametrize("ns,prec,io64", [((24, 16, 8), 64, True), ((24, 16, 8), 32, True), ((24, 16, 8), 32, False),
+                                          ((9, 12, 16), 32, False), ((10, 6, 12), 64, True), ((16, 16, 9), 64, True),
+                                          ((64, 64, 64), 32, False)])
+def test_forward_spectrum(ns, prec, io64):
+    """u_hat = fft(u)/Np against numpy: fields in the compute type go straight through the z pass
+    that writes the full spectrum (odd x lengths, 3 * 2^n lengths); a z length without a
+    compile-time kernel (9) and mixed io/compute types take the half spectrum + scatter form."""
     ks = O.wavenumber_grid(ns, (2 * np.pi,) * 3)
     rng = np.random.default_rng(1)
     u = rng.standard_normal(ns + (3,))
-    plan = F.get_plan(ns, 3, 3, "none", prec, True, ks)
-    got = plan.forward_spectrum(u)
+    plan = F.get_plan(ns, 3, 3, "none", prec, io64, ks)
+    got = plan.forward_spectrum(u if io64 else u.astype(np.float32))
     ref = np.fft.fftn(u, axes=(0, 1, 2)) / np.prod(ns)
     tol = 1e-13 if prec == 64 else 1e-6
     assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
