@@ -295,3 +295,31 @@ def test_fused_host_input_reads_only_kept_modes():
     assert np.array_equal(got, clean)
     _, _, T, _, _ = O.shell_to_shell(u, ks, ("linear", 4.0), "two_thirds")
     assert rel(got, T) < 1e-5
+
+
+@pytest.mark.parametrize("n,deal", [(512, "two_thirds"), (256, "three_halves")])
+def test_fused_shell_to_shell_largest_tiles(n, deal):
+    """The fused pipeline at the transform lengths with their own tiles (512: 2/3 rule at 512^3; 384:
+    the 3/2 rule at 256^3) against the plan's FP64 path on the same device field (device pointers, a
+    few wide shells so that the FP64 path stays short)."""
+    torch = pytest.importorskip("torch")
+    F.clear_plans()
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    ns = (n, n, n)
+    ks = F.wavenumber_grid(ns, (2 * np.pi,) * 3)
+    u = torch.randn((3, n, n, n), device=dev, dtype=torch.complex64, generator=g)
+    edges = np.asarray(F.shell_edges(F.LinearBinning(n / 8.0), F.kmax(ks)), dtype=np.float64)
+    nsh = len(edges) - 1
+    out = {}
+    for prec, mode, field in ((32, F._lib.S2S_BATCHED, u), (64, F._lib.S2S_PLAIN, u.to(torch.complex128))):
+        plan = F.Plan(ns, 3, 3, deal, prec, prec == 64, ks)
+        T = torch.zeros((nsh, nsh), dtype=torch.float64, device=dev)
+        plan.shell_to_shell_device(field.data_ptr(), 0, edges, 7, 0, 0, mode, T.data_ptr(), 0, 0)
+        torch.cuda.synchronize()
+        out[prec] = T.cpu().numpy()
+        del plan, T
+        F.clear_plans()
+    assert np.max(np.abs(out[64])) > 0
+    assert rel(out[32], out[64]) < 1e-5
