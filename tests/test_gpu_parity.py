@@ -323,3 +323,19 @@ def test_fused_shell_to_shell_largest_tiles(n, deal):
         F.clear_plans()
     assert np.max(np.abs(out[64])) > 0
     assert rel(out[32], out[64]) < 1e-5
+
+
+@pytest.mark.parametrize("inv", ["ke", "helicity"])
+def test_fused_shell_to_shell_two_batches(inv):
+    """28 shells at 64^3: more mediators than one batch holds (16), so the sequence runs two batches;
+    the first (eager), second (captured) and third (replayed) calls all equal the FP64 oracle."""
+    F.clear_plans()
+    u, ks = spectrum_field((64, 64, 64), e_config2, seed=9)
+    I = {"ke": F.KineticEnergy(), "helicity": F.Helicity()}[inv]
+    _, _, T, net, _ = O.shell_to_shell(u, ks, ("linear", 2.0), "two_thirds", inv)
+    assert T.shape[0] > 16
+    for _ in range(3):
+        r = F.calculate_shell_to_shell_transfer(u, ks, binning=F.LinearBinning(2.0), invariant=I,
+                                                spectral=F.GB300Spectral(32), execution=F.GB300Execution("batched"))
+        assert rel(r.transfer_matrix, T) < 1e-5
+        assert rel(r.net_transfer, net) < 1e-4
