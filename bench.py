@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "512³ shell-to-shell T(n,m)/s & HBM GB/s: FP32-batched vs FP64 plain, rel err 1e-5"
 UNIT = "T(n,m)/s"
+FALLBACK_BF16_TFLOPS = 1900.0
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -199,6 +200,35 @@ def read_peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def read_bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["bf16_tflops"]), "measured (burst)"
+    except Exception:
+        return FALLBACK_BF16_TFLOPS, "fallback"
+
+
+def prof_roofline(F, fn, sync):
+    """Per-kernel CUDA-event breakdown of one eager call of ``fn`` (the library's per-launch events):
+    the dominant kernel's algorithmic bytes over its measured time against the HBM peak."""
+    F._lib.prof_enable(True)
+    fn()
+    sync()
+    prof = F._lib.prof_read_all()
+    F._lib.prof_enable(False)
+    if not prof:
+        return None
+    prof_ms = sum(v[0] for v in prof.values())
+    dname, (dms, dbytes, dn) = max(prof.items(), key=lambda kv: kv[1][0])
+    peak, peak_kind = read_peaks()
+    achieved = dbytes / (dms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "launches_per_step": dn,
+            "avg_launch_ms": dms / dn, "share_of_step": dms / prof_ms, "traffic": None,
+            "all_kernels": {k: {"ms": v[0], "GBps": v[1] / (v[0] / 1e3) / 1e9 if v[0] > 0 else None,
+                                "launches": v[2]} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
 
 
 def read_traffic(kernel):
@@ -541,6 +571,15 @@ def run_closure(args):
         del d, m
         torch.cuda.empty_cache()
     headline = results["16"]
+    bf16, bf16_kind = read_bf16_peak()
+    hbm, hbm_kind = read_peaks()
+    tfl = headline["inference_tflops"]
+    io_gbs = n * (9 * 4 + 4) / (headline["inference_ms"] / 1e3) / 1e9   # 9 FP32 inputs, 1 FP32 flux per point
+    roofline = {"bound": "tensor", "kernel": "mlp_forward (tcgen05, BF16 operands, FP32 accumulation)",
+                "achieved": tfl, "peak": bf16, "unit": "TFLOP/s", "frac": tfl / bf16, "peak_source": bf16_kind,
+                "flop_per_point": flop_pt, "traffic": None,
+                "hbm": {"achieved": io_gbs, "peak": hbm, "unit": "GB/s", "frac": io_gbs / hbm,
+                        "bytes_per_point": 40, "peak_source": hbm_kind}}
     line = {"metric": "learned closure: inference points/s, Pi_ell correlation and rel L2 vs exact coarse-graining "
                       "flux (256^3 forced NS, Gaussian k_c = 16)",
             "value": headline["inference_points_per_s"], "unit": "points/s", "n_gpus": 1, "steps": 10,
@@ -552,6 +591,7 @@ def run_closure(args):
                                    (", residual over the gradient model" if args.mixed else "") +
                                    ") trained on z < N/2, scored on z >= N/2",
                        "seed": args.seed},
+            "roofline": roofline,
             "evolve": {"ms_per_rk3_step": evolve_ms, "launches_per_step": evolve_launches, "energy": energy},
             "flop_per_point": flop_pt, "results": results}
     print(json.dumps(line), flush=True)
@@ -662,6 +702,7 @@ def run_batch(args):
     launches = (F.launch_count() - l0) / (args.steps + max(3, args.warmup))
     clocks = clk.stop()
     ms_eager = timed(b32.run_eager, args.steps)
+    roofline = prof_roofline(F, b32.run_eager, torch.cuda.synchronize)
     r32 = b32.results()
     info = b32.info()
     # same set, default kernels (autotuner off), graph
@@ -717,7 +758,7 @@ def run_batch(args):
                                    "isotropic / perpendicular / parallel shells, LinearBinning(1), 2/3 rule",
                        "seed": args.seed, "instances": desc, "modes_total": modes,
                        "l2": "inputs cycle through ~%.1f GB per launch (> 129 MB L2)" % (h2d / 1e9)},
-            "modes_per_s": modes / (ms_graph / 1e3),
+            "roofline": roofline, "modes_per_s": modes / (ms_graph / 1e3),
             "graph": {"kernels": info["graph_kernels"], "branches": info["branches"]},
             "ms_sequential_eager_autotuned": ms_eager, "ms_graph_default_kernels": ms_graph_untuned,
             "speedup_graph_vs_sequential": ms_eager / ms_graph,
@@ -902,6 +943,12 @@ def run_padded(args):
     launches = (F.launch_count() - l0) / (args.steps + max(3, args.warmup))
     T32 = T.cpu().numpy().copy()
     net32 = net.cpu().numpy().copy()
+
+    def eager():
+        with torch.cuda.stream(stream):
+            step()
+
+    roofline = prof_roofline(F, eager, torch.cuda.synchronize)
     del plan
     F.clear_plans()
     torch.cuda.empty_cache()
@@ -920,7 +967,7 @@ def run_padded(args):
             "config": {"workload": f"256^3 D=3 {nsh}-shell shell-to-shell, LinearBinning(7), PaddedThreeHalves "
                                    "(384^3 transforms), E ~ k^4 exp(-2(k/8)^2), FP32-batched with FP64 sums",
                        "seed": args.seed},
-            "fp64_plain_ms": ms64, "speedup_vs_fp64_plain": ms64 / ms,
+            "roofline": roofline, "fp64_plain_ms": ms64, "speedup_vs_fp64_plain": ms64 / ms,
             "rel_err_vs_fp64_maxnorm": float(np.max(np.abs(T32 - T64n)) / scale),
             "per_shell_rel_err_max_over_shells_with_transfer": float(np.max(
                 (np.abs(T32 - T64n).max(axis=0) / np.maximum(np.abs(T64n).max(axis=0), 1e-300))[
@@ -977,12 +1024,18 @@ def run_m2m(args):
     T = Tt.cpu().numpy().T            # the library writes T(n, m) column-major
     scale = np.max(np.abs(T))
     head = res["fp64_products"]
+    hbm, hbm_kind = read_peaks()
+    roofline = {"bound": "hbm", "kernel": "mode_to_mode (FP64 products)", "achieved": head["GBps_S_write"],
+                "peak": hbm, "unit": "GB/s", "frac": head["GBps_S_write"] / hbm, "peak_source": hbm_kind,
+                "algorithmic_bytes_per_launch": 8.0 * nm * nm, "traffic": None,
+                "note": "bytes = the FP64 S matrix written once; the kernel is bound by its triad products "
+                        "(FP64 arithmetic), not by that write"}
     line = {"metric": "32^3 resolved mode-to-mode S(k|p): pairs/s (FP64 sums)", "value": head["pairs_per_s"],
             "unit": "pairs/s", "n_gpus": 1, "steps": max(1, args.steps), "warmup": 2, "ms_per_step": head["ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "32^3 D=3 S(k|p) over all 32768^2 mode pairs, OrszagTwoThirds, E ~ k^4 exp(-2(k/8)^2)",
                        "seed": args.seed},
-            "forms": res, "shell_sum_vs_shell_to_shell_rel": float(np.max(np.abs(Tsum - T)) / scale),
+            "roofline": roofline, "forms": res, "shell_sum_vs_shell_to_shell_rel": float(np.max(np.abs(Tsum - T)) / scale),
             "S_antisymmetry_rel": float((S + S.t()).abs().max().item() / S.abs().max().item()),
             "net_sum_rel": float(abs(net.sum().item()) / net.abs().sum().item())}
     print(json.dumps(line), flush=True)
