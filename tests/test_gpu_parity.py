@@ -297,11 +297,13 @@ def test_fused_host_input_reads_only_kept_modes():
     assert rel(got, T) < 1e-5
 
 
-@pytest.mark.parametrize("n,deal", [(512, "two_thirds"), (256, "three_halves")])
+@pytest.mark.parametrize("n,deal", [(512, "two_thirds"), (256, "three_halves"), (128, "three_halves"),
+                                    (512, "three_halves")])
 def test_fused_shell_to_shell_largest_tiles(n, deal):
     """The fused pipeline at the transform lengths with their own tiles (512: 2/3 rule at 512^3; 384:
-    the 3/2 rule at 256^3) against the plan's FP64 path on the same device field (device pointers, a
-    few wide shells so that the FP64 path stays short)."""
+    the 3/2 rule at 256^3) and at the other 3/2 lengths (192 at 128^3, 768 at 512^3: two mediators
+    per batch) against the plan's FP64 path on the same device field (device pointers, a few wide
+    shells so that the FP64 path stays short)."""
     torch = pytest.importorskip("torch")
     F.clear_plans()
     dev = torch.device("cuda", 0)
