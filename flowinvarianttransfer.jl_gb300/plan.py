@@ -181,6 +181,12 @@ class Plan:
                                                       len(e), dmask, int(coord_f32), self._vp(out), PTR_HOST))
         return out.reshape(len(invs), 8, n)
 
+    def spectral_flux_device(self, u_ptr, a_ptr, c_ptr, edges, dmask, coord_f32, inv, T_ptr, P_ptr):
+        e = np.ascontiguousarray(edges, dtype=np.float64)
+        check(self.lib.fit_spectral_flux(self.h, C.c_void_p(u_ptr), C.c_void_p(a_ptr) if a_ptr else None,
+                                         C.c_void_p(c_ptr) if c_ptr else None, _dptr(e), len(e), dmask,
+                                         int(coord_f32), inv, C.c_void_p(T_ptr), C.c_void_p(P_ptr), PTR_DEVICE))
+
     def partial_fluxes_device(self, u_ptr, decomposition, inv, edges, dmask, coord_f32, T_ptr):
         e = np.ascontiguousarray(edges, dtype=np.float64)
         check(self.lib.fit_partial_fluxes(self.h, C.c_void_p(u_ptr), decomposition, inv, _dptr(e), len(e), dmask,
