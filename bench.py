@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--decomp", default="helical", choices=["helical", "toroidal_poloidal"],
                     help="partial config: the decomposition of the velocity into two components")
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--branches", type=int, default=8, help="batch config: concurrent graph branches")
     ap.add_argument("--closure-n", type=int, default=256)
     ap.add_argument("--closure-nsteps", type=int, default=200)
     ap.add_argument("--train-steps", type=int, default=1500)
@@ -682,7 +683,7 @@ def run_batch(args):
         return e0.elapsed_time(e1) / reps
 
     F.autotune_clear()
-    b32 = F.SpectralFluxBatch(specs32, precision=32, n_branches=4, autotune=True)
+    b32 = F.SpectralFluxBatch(specs32, precision=32, n_branches=args.branches, autotune=True)
     t0 = time.perf_counter()
     b32.run()                                      # eager: allocation + autotuning
     torch.cuda.synchronize()
@@ -707,7 +708,7 @@ def run_batch(args):
     info = b32.info()
     # same set, default kernels (autotuner off), graph
     F.autotune_enable(False)
-    bnt = F.SpectralFluxBatch(specs32, precision=32, n_branches=4, autotune=False)
+    bnt = F.SpectralFluxBatch(specs32, precision=32, n_branches=args.branches, autotune=False)
     bnt.run()
     bnt.run()
     ms_graph_untuned = timed(bnt.run, args.steps)

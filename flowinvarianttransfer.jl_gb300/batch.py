@@ -44,7 +44,7 @@ class SpectralFluxBatch:
     sums; 64 is FP64 throughout. The first :meth:`run` executes eagerly (allocation, autotuning),
     the second captures and launches the graph, later runs launch it."""
 
-    def __init__(self, instances, precision=32, n_branches=4, autotune=True):
+    def __init__(self, instances, precision=32, n_branches=8, autotune=True):
         torch = _torch()
         self.lib = _lib.load()
         self.precision = int(precision)
@@ -134,7 +134,7 @@ class SpectralFluxBatch:
             pass
 
 
-def calculate_spectral_flux_batch(instances, precision=32, n_branches=4, autotune=True):
+def calculate_spectral_flux_batch(instances, precision=32, n_branches=8, autotune=True):
     """Spectral flux of every instance (see :class:`SpectralFluxBatch`), one graph launch for all."""
     b = SpectralFluxBatch(instances, precision=precision, n_branches=n_branches, autotune=autotune)
     b.run()
