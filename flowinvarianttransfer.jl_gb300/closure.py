@@ -11,7 +11,7 @@
   (6 targets) and the exact flux ``Pi_ell``.
 * ``SubfilterStressMLP`` is the learned closure: a pointwise 9 -> 64 -> 64 -> 6 network trained and
   evaluated with the library's BF16 tensor-core kernels (FP32 accumulation). The exact
-  coarse-graining path stays its fallback and the judge of its error.
+  coarse-graining path stays its fallback and the reference for its error.
 
 Device data is held in torch tensors (allocation and streams only); every computation is a call
 into libfit_gb300.

@@ -207,7 +207,7 @@ def test_mode_to_mode_triad_3d_nodealias_and_helicity():
             assert np.allclose(a, b, atol=1e-12 * (np.abs(a).max() + 1e-300))
 
 
-def test_shell_edges_rules():                           # ShellBinning.jl:50-79, SURVEY facts 5-6
+def test_shell_edges_rules():                           # ShellBinning.jl:50-79
     ks = kgrid((64, 64))
     kc, edges, centers, sidx = O.shell_setup(ks, ("linear", 1.0))
     assert len(centers) == 46 and edges[-1] == kc.max()
