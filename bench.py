@@ -1197,6 +1197,12 @@ def run_frontend(args):
         torch.mul(torch.fft.fftn(u, dim=(1, 2, 3)), inv, out=res)
 
     ms_cufft = _timed_ms(cufft_step, stream, args.steps, warm=max(3, args.warmup))
+
+    def eager():
+        with torch.cuda.stream(stream):
+            step()
+
+    passes = prof_roofline(F, eager, torch.cuda.synchronize)
     alg = 3.0 * N ** 3 * (4 + 8)
     peak, peak_kind = read_peaks()
     line = {"metric": f"{N}^3 physical-space front end u_hat = fft(u)/Np, 3 real FP32 fields: fields/s",
@@ -1208,6 +1214,7 @@ def run_frontend(args):
             "roofline": {"bound": "hbm", "kernel": "whole call", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
                          "algorithmic_bytes": alg, "traffic": None},
+            "passes": None if passes is None else passes["all_kernels"],
             "cufft_fftn_ms": ms_cufft, "speedup_vs_cufft": ms_cufft / ms,
             "rel_err_vs_cufft_maxnorm": err, "gpu_launches": int(launches)}
     print(json.dumps(line), flush=True)

@@ -30,7 +30,8 @@ static size_t g_prof_used = 0;
 static bool g_prof_enabled = false;
 static const char* g_prof_names[PK_COUNT] = {"fft_strided", "fft_c2r_x", "fft_r2c_x", "gather", "product",
                                              "bin", "carrier", "triad", "shell_table", "s2s_zinv", "s2s_yinv",
-                                             "s2s_xmix", "s2s_yfwd", "s2s_zfwd_bin", "s2s_velocity"};
+                                             "s2s_xmix", "s2s_yfwd", "s2s_zfwd_bin", "s2s_velocity",
+                                             "fft_z_full"};
 
 static cudaEvent_t prof_event() {
   if (g_prof_used < g_prof_pool.size()) return g_prof_pool[g_prof_used++];

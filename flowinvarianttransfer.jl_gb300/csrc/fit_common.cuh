@@ -76,7 +76,8 @@ long fit_launch_total();
 // launch's algorithmic DRAM bytes; read back through fit_prof_read().
 enum ProfKind {
   PK_FFT_STRIDED = 0, PK_FFT_C2R_X, PK_FFT_R2C_X, PK_GATHER, PK_PRODUCT, PK_BIN, PK_CARRIER, PK_TRIAD,
-  PK_SHELL, PK_S2S_ZINV, PK_S2S_YINV, PK_S2S_XMIX, PK_S2S_YFWD, PK_S2S_ZFWD_BIN, PK_S2S_VELOCITY, PK_COUNT
+  PK_SHELL, PK_S2S_ZINV, PK_S2S_YINV, PK_S2S_XMIX, PK_S2S_YFWD, PK_S2S_ZFWD_BIN, PK_S2S_VELOCITY, PK_FFT_Z_FULL,
+  PK_COUNT
 };
 bool fit_prof_on();
 void fit_prof_begin(int kind, double bytes, cudaStream_t st);

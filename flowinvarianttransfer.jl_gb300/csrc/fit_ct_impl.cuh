@@ -62,7 +62,7 @@ static int ct_z_full_n(const V* in, V* out, int N0, int Mh0, int N1, long Q, con
 template <typename V, int N>
 static int ct_c2r_n(const V* in, typename Scal<V>::t* out, long L, typename Scal<V>::t scale, const V* tw,
                     cudaStream_t st) {
-  typedef CtTile<V, N> TT;
+  typedef CtXTile<V, N> TT;
   const long grid = (L + 2L * TT::C - 1) / (2L * TT::C);
   FIT_TRY(ct_prep(k_ct_c2r_x<V, N>, TT::SMEM, TT::NTHR));
   k_ct_c2r_x<V, N><<<(unsigned)grid, TT::NTHR, TT::SMEM, st>>>(in, out, L, tw, scale);
@@ -72,7 +72,7 @@ static int ct_c2r_n(const V* in, typename Scal<V>::t* out, long L, typename Scal
 template <typename V, int N>
 static int ct_r2c_n(const typename Scal<V>::t* in, V* out, long L, typename Scal<V>::t scale, const V* tw,
                     cudaStream_t st) {
-  typedef CtTile<V, N> TT;
+  typedef CtXTile<V, N> TT;
   const long grid = (L + 2L * TT::C - 1) / (2L * TT::C);
   FIT_TRY(ct_prep(k_ct_r2c_x<V, N>, TT::SMEM, TT::NTHR));
   k_ct_r2c_x<V, N><<<(unsigned)grid, TT::NTHR, TT::SMEM, st>>>(in, out, L, tw, scale);

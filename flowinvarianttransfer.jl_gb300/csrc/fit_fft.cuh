@@ -344,6 +344,20 @@ struct CtTile {
   static constexpr int MINB = NTHR >= 768 ? 2 : (NTHR >= 512 ? 3 : 4);
 };
 
+// Tile of the x passes (real <-> half spectrum along contiguous lines): their staged loads and the
+// real-pair split are coalesced for any column count, so a 16-column tile that would need more than
+// 512 threads is halved (block-wide barriers over fewer warps, more resident blocks).
+template <typename V, int N>
+struct CtXTile {
+  static constexpr int VB = (int)sizeof(V);
+  static constexpr int C = (CtTile<V, N>::C >= 16 && CtTile<V, N>::NTHR > 512) ? CtTile<V, N>::C / 2
+                                                                             : CtTile<V, N>::C;
+  static constexpr int E = C * N;
+  static constexpr int EPT = E <= 8192 ? 8 : 16;
+  static constexpr int NTHR = (E / EPT + 31) / 32 * 32;
+  static constexpr size_t SMEM = (size_t)(E + N) * VB;
+};
+
 template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS>
 __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
   constexpr int MAXB = (EPT + R - 1) / R;
@@ -478,11 +492,11 @@ __global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_z_full(const V* __res
 }
 
 template <typename V, int N>
-__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_c2r_x(const V* __restrict__ in,
+__global__ void __launch_bounds__(CtXTile<V, N>::NTHR) k_ct_c2r_x(const V* __restrict__ in,
                                                                 typename Scal<V>::t* __restrict__ out, long L,
                                                                 const V* __restrict__ twg,
                                                                 typename Scal<V>::t scale) {
-  typedef CtTile<V, N> TT;
+  typedef CtXTile<V, N> TT;
   constexpr int C = TT::C, E = TT::E, Nh = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   V* s = reinterpret_cast<V*>(fit_smem_raw);
@@ -523,11 +537,11 @@ __global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_c2r_x(const V* __rest
 }
 
 template <typename V, int N>
-__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_r2c_x(const typename Scal<V>::t* __restrict__ in,
+__global__ void __launch_bounds__(CtXTile<V, N>::NTHR) k_ct_r2c_x(const typename Scal<V>::t* __restrict__ in,
                                                                 V* __restrict__ out, long L,
                                                                 const V* __restrict__ twg,
                                                                 typename Scal<V>::t scale) {
-  typedef CtTile<V, N> TT;
+  typedef CtXTile<V, N> TT;
   typedef typename Scal<V>::t S;
   constexpr int C = TT::C, E = TT::E, Nh = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];

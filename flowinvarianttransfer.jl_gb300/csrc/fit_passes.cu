@@ -575,7 +575,7 @@ int forward_nd_full(const T* phys, typename Vec2<T>::t* half, typename Vec2<T>::
   const long Mh0 = g.Mh0, M1 = g.M[1], M2 = g.M[2];
   FIT_TRY(pass_r2c_x<T>(phys, half, ax[0], M1 * M2 * nf, scale, st));
   FIT_TRY(pass_strided<T>(half, half, ax[1], Mh0, M2 * nf, false, (T)1, st));
-  fit_prof_begin(PK_FFT_STRIDED, (double)nf * Mh0 * M1 * M2 * sizeof(typename Vec2<T>::t) * 3.0, st);
+  fit_prof_begin(PK_FFT_Z_FULL, (double)nf * Mh0 * M1 * M2 * sizeof(typename Vec2<T>::t) * 3.0, st);
   const int rc = ct_z_full<T>(half, full, g.M[0], (int)Mh0, (int)M1, n2, nf, axis_tw<T>(ax[2]), st);
   fit_prof_end(st);
   if (rc != FIT_OK) return rc == 1 ? FIT_ERR_SIZE : rc;

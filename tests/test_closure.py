@@ -435,3 +435,22 @@ def test_learned_closure_gain():
     # the residual network keeps the gradient model's accuracy and adds to it
     ev = res[(True, True)]
     assert ev["rel_l2_mlp"] <= ev["rel_l2_gradient_model"] * 1.02
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ns", [(512, 8, 8), (768, 6, 4)])
+def test_x_passes_long_lines_fp32(ns):
+    """The real <-> half x passes at lengths whose FP32 tile is halved to 8 columns (512, 768): the
+    forward spectrum against numpy, and the plain FP32 nonlinear term (its inverse x pass) against
+    the FP64 plan's."""
+    ks = O.wavenumber_grid(ns, (2 * np.pi,) * 3)
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal(ns + (3,))
+    plan = F.get_plan(ns, 3, 3, "none", 32, False, ks)
+    got = plan.forward_spectrum(u.astype(np.float32))
+    ref = np.fft.fftn(u, axes=(0, 1, 2)) / np.prod(ns)
+    assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max()
+    n32 = F.compute_nonlinear_term(ref.astype(np.complex64), ks, dealiasing=F.OrszagTwoThirds(),
+                                   spectral=F.GB300Spectral(32))
+    n64 = F.compute_nonlinear_term(ref, ks, dealiasing=F.OrszagTwoThirds(), spectral=F.GB300Spectral(64))
+    assert np.abs(n32 - n64).max() <= 1e-5 * np.abs(n64).max()
