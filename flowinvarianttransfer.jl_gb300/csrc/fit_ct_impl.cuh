@@ -33,7 +33,7 @@ static int ct_prep(K kern, size_t smem, int nthr) {
 
 template <typename V, bool INV, int N>
 static int ct_strided_n(const V* in, V* out, long P, long Q, typename Scal<V>::t scale, const V* tw, cudaStream_t st) {
-  typedef CtTile<V, N> TT;
+  typedef CtXTile<V, N> TT;
   const long tpq = (P + TT::C - 1) / TT::C;
   const long grid = tpq * Q;
   if (grid > 2147483647L) {

@@ -344,9 +344,11 @@ struct CtTile {
   static constexpr int MINB = NTHR >= 768 ? 2 : (NTHR >= 512 ? 3 : 4);
 };
 
-// Tile of the x passes (real <-> half spectrum along contiguous lines): their staged loads and the
-// real-pair split are coalesced for any column count, so a 16-column tile that would need more than
-// 512 threads is halved (block-wide barriers over fewer warps, more resident blocks).
+// Tile of the stand-alone passes (x: real <-> half spectrum along contiguous lines; strided y and z):
+// a 16-column tile that would need more than 512 threads is halved (block-wide barriers over fewer
+// warps, several resident blocks instead of one). The x passes' staged loads and real-pair split are
+// coalesced for any column count; the strided passes still read 64-byte row runs. The z pass that
+// stores the full spectrum keeps 16 columns: its conjugate-mirror stores want the longer runs.
 template <typename V, int N>
 struct CtXTile {
   static constexpr int VB = (int)sizeof(V);
@@ -410,10 +412,10 @@ __device__ __forceinline__ void ct_stages(V* s, const V* tw, int tid) {
 }
 
 template <typename V, bool INV, int N>
-__global__ void __launch_bounds__(CtTile<V, N>::NTHR) k_ct_strided(const V* in, V* out, long P, long tilesPerQ,
+__global__ void __launch_bounds__(CtXTile<V, N>::NTHR) k_ct_strided(const V* in, V* out, long P, long tilesPerQ,
                                                                   const V* __restrict__ twg,
                                                                   typename Scal<V>::t scale) {
-  typedef CtTile<V, N> TT;
+  typedef CtXTile<V, N> TT;
   constexpr int C = TT::C, E = TT::E;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   V* s = reinterpret_cast<V*>(fit_smem_raw);
