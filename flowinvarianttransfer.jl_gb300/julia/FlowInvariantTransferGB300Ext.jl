@@ -8,15 +8,19 @@
 #   include("FlowInvariantTransferGB300Ext.jl"); using .FlowInvariantTransferGB300Ext: GB300Spectral, GB300Execution
 #   calculate_spectral_flux(û, ks; spectral=GB300Spectral(), binning=LinearBinning(1.0))
 #   calculate_shell_to_shell_transfer(û, ks; spectral=GB300Spectral(:fp32), execution=GB300Execution())
+#   calculate_partial_fluxes(GB300Array(û; spectral=GB300Spectral(:fp32)), ks; binning=DyadicBinning(1.0))
+#   calculate_band_to_band_transfer(GB300Array(û), ks; bands=SmoothBands([2.0, 4.0, 8.0]))
 module FlowInvariantTransferGB300Ext
 
 using FlowInvariantTransfer: FlowInvariantTransfer as FET
 using FlowInvariantTransfer.Types: AbstractSpectralBackend, AbstractExecutionBackend, AbstractDealiasing,
     NoDealiasing, OrszagTwoThirds, PaddedThreeHalves, AbstractInvariant, KineticEnergy, PassiveScalar, Helicity,
     Enstrophy, ShellToShellResult, ShellMagnitude
-using FlowInvariantTransfer.ShellBinning: shell_edges, shell_coordinate
+using FlowInvariantTransfer.ShellBinning: shell_edges, shell_centers, shell_coordinate
+using FlowInvariantTransfer.Types: HelicalDecomposition, HelmholtzDecomposition, ToroidalPoloidalDecomposition,
+    SmoothBands, IsotropicShells, SpectralFluxResult, ModeToModeTriadResult
 
-export GB300Spectral, GB300Execution
+export GB300Spectral, GB300Execution, GB300Array
 
 const LIB = get(ENV, "FIT_GB300_LIB", "libfit_gb300")
 
@@ -134,6 +138,100 @@ function FET.SpectralFlux._calculate_spectral_flux_decomposed(û_decomp::Abstrac
         _inv(invariant), T, Π, 0))
     FT = real(eltype(velocity_hat))
     return FET.Types.SpectralFluxResult(centers, FT.(T), FT.(Π))
+end
+
+# 4. reference functions whose backend is a keyword only (src/SpectralFlux.jl:240-285,
+# src/ScaleToScale/ScaleToScaleTransfer.jl:49-91, src/BandTransfer.jl:65-113) dispatch on the
+# array: a field wrapped in GB300Array runs them in libfit_gb300.
+"""
+    GB300Array(û; spectral=GB300Spectral())
+
+A spectral field (column-major `(ns..., comp)`, interleaved complex) marked for the GB300 backend.
+`calculate_partial_fluxes`, `calculate_mode_to_mode_transfer` and `calculate_band_to_band_transfer`
+called on it run in libfit_gb300 and return the reference's result types.
+"""
+struct GB300Array{T, N, A <: AbstractArray{T, N}} <: AbstractArray{T, N}
+    data::A
+    spectral::GB300Spectral
+end
+GB300Array(A::AbstractArray; spectral=GB300Spectral()) = GB300Array{eltype(A), ndims(A), typeof(A)}(A, spectral)
+Base.size(a::GB300Array) = size(a.data)
+Base.getindex(a::GB300Array, i...) = getindex(a.data, i...)
+Base.unsafe_convert(::Type{Ptr{T}}, a::GB300Array) where {T} = Base.unsafe_convert(Ptr{T}, a.data)
+Base.cconvert(::Type{Ptr{Cvoid}}, a::GB300Array) = a.data
+
+_decomp(::HelicalDecomposition) = (Cint(1), (:positive, :negative))
+_decomp(::HelmholtzDecomposition) = (Cint(2), (:rotational, :divergent))
+_decomp(::ToroidalPoloidalDecomposition) = (Cint(3), (:toroidal, :poloidal))
+_coord32(ks) = eltype(ks[1]) == Float32 ? Cint(1) : Cint(0)
+
+function FET.SpectralFlux.calculate_partial_fluxes(velocity_hat::GB300Array, ks;
+        decomposition=HelicalDecomposition(), binning=FET.SpectralFlux._default_binning(ks),
+        dealiasing=OrszagTwoThirds(), spectral=velocity_hat.spectral, geometry=IsotropicShells())
+    û = velocity_hat.data
+    p = _plan(û, ks, dealiasing, spectral isa GB300Spectral ? spectral : velocity_hat.spectral)
+    code, names = _decomp(decomposition)
+    κ = shell_coordinate(geometry, ks)
+    edges = Vector{Float64}(shell_edges(binning, maximum(κ)))
+    centers = collect(shell_centers(binning, maximum(κ)))
+    nsh = length(edges) - 1
+    Tc = Vector{Float64}(undef, 8 * nsh)
+    _check(ccall((:fit_partial_fluxes, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Cint, UInt32, Cint, Ptr{Float64}, Cint),
+        p.ptr, û, code, Cint(0), edges, length(edges), _dims_mask(geometry, length(ks)), _coord32(ks), Tc, 0))
+    FT = real(eltype(û))
+    channels = Dict{NTuple{3, Symbol}, SpectralFluxResult}()
+    for (ik, sk) in enumerate(names), (ip, sp) in enumerate(names), (iq, sq) in enumerate(names)
+        off = ((ik - 1) * 4 + (ip - 1) * 2 + (iq - 1)) * nsh
+        T = FT.(Tc[off+1:off+nsh])
+        channels[(sk, sp, sq)] = SpectralFluxResult(centers, T, cumsum(T))
+    end
+    total = SpectralFluxResult(centers, sum(c.transfer_spectrum for c in values(channels)),
+                               sum(c.flux for c in values(channels)))
+    return (channels = channels, total = total, k_shells = centers)
+end
+
+function FET.ScaleToScaleTransfer.calculate_mode_to_mode_transfer(velocity_hat::GB300Array, ks;
+        invariant=KineticEnergy(),
+        dealiasing=OrszagTwoThirds(), spectral=velocity_hat.spectral, max_modes::Int=1024, force::Bool=false,
+        advecting_hat=velocity_hat)
+    û = velocity_hat.data
+    nd = length(ks)
+    ns = size(û)[1:nd]
+    nm = prod(ns)
+    (force || nm <= max_modes) || throw(ArgumentError(
+        "calculate_mode_to_mode_transfer resolves S(k|p) over all $(nm)x$(nm) mode pairs; N_modes=$nm exceeds " *
+        "max_modes=$max_modes (pass force=true)."))
+    adv = advecting_hat isa GB300Array ? advecting_hat.data : advecting_hat
+    p = _plan(û, ks, dealiasing, spectral isa GB300Spectral ? spectral : velocity_hat.spectral; advecting=adv)
+    S = Array{Float64}(undef, ns..., ns...)
+    net = Array{Float64}(undef, ns...)
+    _check(ccall((:fit_mode_to_mode, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint),
+        p.ptr, û, adv === û ? C_NULL : adv, _inv(invariant), Cint(1), S, net, 0))
+    FT = real(eltype(û))
+    return ModeToModeTriadResult(invariant, ks, FT.(net), FT.(S))
+end
+
+function FET.BandTransfer.calculate_band_to_band_transfer(velocity_hat::GB300Array, ks; bands::SmoothBands,
+        dealiasing=OrszagTwoThirds(), invariant=KineticEnergy(), spectral=velocity_hat.spectral,
+        advecting_hat=velocity_hat, geometry=IsotropicShells())
+    û = velocity_hat.data
+    adv = advecting_hat isa GB300Array ? advecting_hat.data : advecting_hat
+    p = _plan(û, ks, dealiasing, spectral isa GB300Spectral ? spectral : velocity_hat.spectral; advecting=adv)
+    centers = Vector{Float64}(bands.centers)
+    nb = length(centers)
+    T = Matrix{Float64}(undef, nb, nb)
+    net = Vector{Float64}(undef, nb)
+    asym = Ref{Float64}(NaN)
+    _check(ccall((:fit_band_to_band, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Cint, Cdouble, UInt32, Cint, Cint, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}, Cint),
+        p.ptr, û, adv === û ? C_NULL : adv, centers, nb, Float64(bands.logwidth), _dims_mask(geometry, length(ks)),
+        _coord32(ks), _inv(invariant), T, net, asym, 0))
+    FT = real(eltype(û))
+    return (centers = collect(bands.centers), transfer_matrix = FT.(T), net_transfer = FT.(net),
+            max_antisymmetry_error = FT(asym[]))
 end
 
 end # module
