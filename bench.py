@@ -227,9 +227,11 @@ def prof_roofline(F, fn, sync):
     achieved = dbytes / (dms / 1e3) / 1e9
     return {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "launches_per_step": dn,
-            "avg_launch_ms": dms / dn, "share_of_step": dms / prof_ms, "traffic": None,
+            "algorithmic_bytes_per_launch": dbytes / dn, "avg_launch_ms": dms / dn,
+            "share_of_step": dms / prof_ms, "traffic": None,
             "all_kernels": {k: {"ms": v[0], "GBps": v[1] / (v[0] / 1e3) / 1e9 if v[0] > 0 else None,
-                                "launches": v[2]} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+                                "launches": v[2]} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+            "step_alg_bytes_GB": sum(v[1] for v in prof.values()) / 1e9}
 
 
 def read_traffic(kernel):
@@ -828,24 +830,12 @@ def run_partial(args):
         clocks = clk.stop()
     ms = e0.elapsed_time(e1) / args.steps
     T32 = T.cpu().numpy().reshape(2, 8, nsh).copy()
-    # per-kernel breakdown of one eager pass (CUDA events around each launch)
-    F._lib.prof_enable(True)
-    with torch.cuda.stream(stream):
-        step()
-    torch.cuda.synchronize()
-    prof = F._lib.prof_read_all()
-    F._lib.prof_enable(False)
-    prof_ms = sum(v[0] for v in prof.values())
-    dname, (dms, dbytes, dn) = max(prof.items(), key=lambda kv: kv[1][0])
-    peak, peak_kind = read_peaks()
-    achieved = dbytes / (dms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "launches_per_step": dn,
-                "algorithmic_bytes_per_launch": dbytes / dn, "avg_launch_ms": dms / dn, "traffic": None,
-                "share_of_step": dms / prof_ms,
-                "all_kernels": {k: {"ms": v[0], "GBps": v[1] / (v[0] / 1e3) / 1e9 if v[0] > 0 else None,
-                                    "launches": v[2]} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
-                "step_alg_bytes_GB": sum(v[1] for v in prof.values()) / 1e9}
+
+    def eager():   # per-kernel breakdown of one eager pass (CUDA events around each launch)
+        with torch.cuda.stream(stream):
+            step()
+
+    roofline = prof_roofline(F, eager, torch.cuda.synchronize)
     # plain per-invariant path, FP32 (one call per invariant, four nonlinear terms each)
     Tp = torch.zeros(8 * nsh, dtype=torch.float64, device=dev)
     with torch.cuda.stream(stream):
@@ -1098,21 +1088,11 @@ def run_band(args):
     ms = e0.elapsed_time(e1) / args.steps
     T32 = T.cpu().numpy().T.copy()   # T(n, m) column-major on the device
     asym32 = float(asym.item())
-    F._lib.prof_enable(True)
-    with torch.cuda.stream(stream):
-        run(plan, u, T)
-    torch.cuda.synchronize()
-    prof = F._lib.prof_read_all()
-    F._lib.prof_enable(False)
-    prof_ms = sum(v[0] for v in prof.values())
-    dname, (dms, dbytes, dn) = max(prof.items(), key=lambda kv: kv[1][0])
-    peak, peak_kind = read_peaks()
-    achieved = dbytes / (dms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "launches_per_step": dn,
-                "avg_launch_ms": dms / dn, "share_of_step": dms / prof_ms, "traffic": None,
-                "all_kernels": {k: {"ms": v[0], "GBps": v[1] / (v[0] / 1e3) / 1e9 if v[0] > 0 else None,
-                                    "launches": v[2]} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+    def eager():
+        with torch.cuda.stream(stream):
+            run(plan, u, T)
+
+    roofline = prof_roofline(F, eager, torch.cuda.synchronize)
     del plan
     F.clear_plans()
     torch.cuda.empty_cache()
