@@ -669,12 +669,11 @@ def band_weights(centers, logwidth, kcoord):
     ``kappa <= 0``."""
     kappa = np.asarray(kcoord, dtype=np.float64)
     pos = kappa > 0
+    kp = np.where(pos, kappa, 1.0)
     W = []
-    with np.errstate(divide="ignore", invalid="ignore"):
-        lk = np.log(np.where(pos, kappa, 1.0))
-        for c in centers:
-            r = lk - np.log(float(c))
-            W.append(np.where(pos, np.exp(-(r * r) / (2.0 * logwidth * logwidth)), 0.0))
+    for c in centers:   # r = ln(kappa / c), exp(-r^2 / (2 sigma sigma)), in the reference's order (:35-36)
+        r = np.log(kp / float(c))
+        W.append(np.where(pos, np.exp(-(r * r) / (2.0 * logwidth * logwidth)), 0.0))
     W = np.stack(W)
     s = W.sum(axis=0)
     return np.where(s > 0, W / np.where(s > 0, s, 1.0), 0.0)

@@ -106,3 +106,18 @@ def test_band_live_box_many_bands_match_plain_path():
     r64 = F.calculate_band_to_band_transfer(u, ks, F.SmoothBands(centers, 0.4), spectral=F.GB300Spectral(64))
     Tn = np.sqrt(np.sum(r64.transfer_matrix ** 2))
     assert np.max(np.abs(r32.transfer_matrix - r64.transfer_matrix)) <= 2e-5 * Tn
+
+
+def test_oracle_band_properties_3d():
+    """3D, self-advection of a Hermitian solenoidal field under the 2/3 rule: antisymmetric and
+    conservative up to rounding, net = row sums, weights a partition of unity off the origin."""
+    from fields import spectrum_field, e_config2
+    u, ks = spectrum_field((16, 16, 16), e_config2, seed=5)
+    centers = [1.5, 3.0, 6.0]
+    _, T, net, asym = O.band_to_band(u, ks, centers, 0.6)
+    Tn = np.sqrt(np.sum(T ** 2))
+    assert Tn > 0 and asym < 1e-10 * Tn and abs(T.sum()) < 1e-10 * Tn
+    assert np.allclose(net, T.sum(axis=1), atol=1e-12 * Tn)
+    kappa = O.shell_coordinate(ks)
+    W = O.band_weights(centers, 0.6, kappa)
+    assert np.allclose(W.sum(axis=0)[kappa > 0], 1.0) and np.all(W[:, kappa == 0] == 0)
