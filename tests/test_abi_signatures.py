@@ -1,0 +1,48 @@
+"""The ctypes declarations of the Python binding agree with the C header: every function declared in
+include/fit_gb300.h that the binding types has the same number of parameters (no GPU needed)."""
+import os
+import re
+
+import fit_gb300 as F
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_params():
+    src = open(os.path.join(ROOT, "include", "fit_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", " ", src)
+    out = {}
+    for m in re.finditer(r"\b(fit_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", src):
+        name, params = m.group(1), m.group(2).strip()
+        out[name] = 0 if params in ("", "void") else len([p for p in params.split(",") if p.strip()])
+    return out
+
+
+class _Fn:
+    argtypes = None
+    restype = None
+
+
+class _FakeLib:
+    def __init__(self):
+        self.fns = {}
+
+    def __getattr__(self, name):
+        if name.startswith("fit_"):
+            return self.fns.setdefault(name, _Fn())
+        raise AttributeError(name)
+
+
+def test_binding_matches_header():
+    hdr = _header_params()
+    assert len(hdr) >= len(F._lib.EXPORTS)
+    for name in F._lib.EXPORTS:
+        assert name in hdr, f"{name} is exported by the binding but not declared in the header"
+    fake = _FakeLib()
+    F._lib._declare(fake)
+    typed = {n: f.argtypes for n, f in fake.fns.items() if f.argtypes is not None}
+    assert len(typed) >= 30
+    for name, args in typed.items():
+        assert name in hdr, name
+        assert len(args) == hdr[name], f"{name}: binding has {len(args)} parameters, header {hdr[name]}"
