@@ -13,7 +13,7 @@ from .api import (compute_nonlinear_term, transfer_density, decompose_field, ass
                   calculate_scalar_shell_to_shell_transfer, calculate_partial_fluxes,
                   calculate_helical_partial_fluxes, calculate_partial_fluxes_multi, calculate_mode_to_mode_transfer,
                   calculate_scalar_mode_to_mode_transfer, calculate_energy_transfer,
-                  calculate_band_to_band_transfer)
+                  calculate_band_to_band_transfer, physical_to_spectral)
 from .plan import Plan, get_plan, clear_plans  # noqa: F401
 from .batch import (SpectralFluxBatch, calculate_spectral_flux_batch, autotune_summary,  # noqa: F401
                     autotune_enable, autotune_clear)

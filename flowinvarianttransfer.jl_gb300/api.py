@@ -12,7 +12,7 @@ import numpy as np
 
 from . import _lib
 from .plan import get_plan
-from .shells import (coord_is_f32, default_binning, dims_mask, kmax, shell_centers, shell_edges)
+from .shells import (coord_is_f32, default_binning, dims_mask, kmax, shell_centers, shell_edges, wavenumber_grid)
 from .types import (BandToBandResult, DivergentDecomposition, DirectSumBackend, Enstrophy, FFTBackend, GB300Execution,
                     GB300Spectral, HelicalDecomposition, HelmholtzDecomposition, Helicity, IsotropicShells,
                     KineticEnergy, ModeToModeTransferMethod, ModeToModeTriadResult, NoDecomposition,
@@ -54,6 +54,49 @@ def _plan(velocity_hat, ks, dealiasing, spectral, advecting_hat):
     io64 = not (v.dtype == np.complex64 and adv.dtype == np.complex64)
     prec = _spec_precision(spectral, v)
     return get_plan(ns, M, D, dealiasing.key, prec, io64, ks)
+
+
+def _physical_stack(velocity_fields):
+    """(ns..., M) real array from a tuple of M component arrays on one grid, or from one array (a
+    single field, M = 1)."""
+    if isinstance(velocity_fields, (tuple, list)):
+        fields = [np.asarray(f) for f in velocity_fields]
+        if not fields:
+            raise ValueError("no fields given")
+        ns = fields[0].shape
+        if any(f.shape != ns for f in fields):
+            raise ValueError("velocity components must share one grid shape")
+        u = np.stack(fields, axis=-1)
+    else:
+        u = np.asarray(velocity_fields)[..., None]
+    if np.iscomplexobj(u):
+        raise ValueError("physical fields must be real")
+    if not 1 <= u.ndim - 1 <= 3:
+        raise ValueError(f"fields of {u.ndim - 1} dimensions; expected 1, 2 or 3")
+    return u
+
+
+def physical_to_spectral(velocity_fields, spectral=GB300Spectral()):
+    """``û = fft(u) ./ Np`` of real physical fields, on the device: the step a caller of the reference
+    performs before every spectral diagnostic (``src/FlowInvariantTransfer.jl:233-243``,
+    ``cat(FFTW.fft(u), FFTW.fft(v); dims=3) ./ N^2``). ``velocity_fields`` is a tuple of real
+    component arrays on one grid, or one real array (a single field). Returns the complex array
+    ``(ns..., M)``: complex128 for FP64 (the default for float64 input), complex64 for FP32."""
+    u = _physical_stack(velocity_fields)
+    ns, M = u.shape[:-1], u.shape[-1]
+    prec = spectral.precision if isinstance(spectral, GB300Spectral) and spectral.precision else \
+        (32 if u.dtype == np.float32 else 64)
+    if prec not in (32, 64):
+        raise ValueError("precision must be 32 or 64")
+    nd = len(ns)
+    ks = wavenumber_grid(ns, (2 * np.pi,) * nd)   # the transform does not depend on the lengths
+    # plans carry 1..3 transformed fields (and at least nd advecting ones, unused here): chunks of 3
+    parts = []
+    for c0 in range(0, M, 3):
+        m = min(3, M - c0)
+        plan = get_plan(ns, m, max(m, nd), "none", prec, prec == 64, ks)
+        parts.append(plan.forward_spectrum(u[..., c0:c0 + m]))
+    return parts[0] if len(parts) == 1 else np.concatenate(parts, axis=-1)
 
 
 def _shells(ks, binning, geometry):

@@ -46,3 +46,21 @@ def test_binding_matches_header():
     for name, args in typed.items():
         assert name in hdr, name
         assert len(args) == hdr[name], f"{name}: binding has {len(args)} parameters, header {hdr[name]}"
+
+
+def test_physical_stack_arguments():
+    """Argument handling of physical_to_spectral (no GPU): component tuples are stacked last, a
+    single array is one field, complex input and mismatched grids are rejected."""
+    import numpy as np
+    import pytest
+    from fit_gb300.api import _physical_stack
+    assert _physical_stack((np.zeros((4, 6)), np.ones((4, 6)))).shape == (4, 6, 2)
+    assert _physical_stack(np.zeros((4, 4, 4))).shape == (4, 4, 4, 1)
+    with pytest.raises(ValueError):
+        _physical_stack((np.zeros((4, 4)), np.zeros((4, 5))))
+    with pytest.raises(ValueError):
+        _physical_stack(np.zeros((4, 4), dtype=np.complex128))
+    with pytest.raises(ValueError):
+        _physical_stack(np.zeros((2, 2, 2, 2)))
+    with pytest.raises(ValueError):
+        _physical_stack(())

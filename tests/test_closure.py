@@ -454,3 +454,23 @@ def test_x_passes_long_lines_fp32(ns):
                                    spectral=F.GB300Spectral(32))
     n64 = F.compute_nonlinear_term(ref, ks, dealiasing=F.OrszagTwoThirds(), spectral=F.GB300Spectral(64))
     assert np.abs(n32 - n64).max() <= 1e-5 * np.abs(n64).max()
+
+
+@pytest.mark.gpu
+def test_physical_to_spectral():
+    """u_hat = fft(u)/Np of real physical fields through the public function, against numpy: one 2D
+    field, two 2D components, four 3D FP32 fields (a chunk of three and one)."""
+    rng = np.random.default_rng(8)
+    u = rng.standard_normal((24, 16))
+    got = F.physical_to_spectral(u)
+    assert got.shape == (24, 16, 1) and got.dtype == np.complex128
+    assert np.abs(got[..., 0] - np.fft.fftn(u) / u.size).max() <= 1e-13 * np.abs(np.fft.fftn(u) / u.size).max()
+    v = rng.standard_normal((24, 16))
+    got = F.physical_to_spectral((u, v))
+    ref = np.stack([np.fft.fftn(u), np.fft.fftn(v)], axis=-1) / u.size
+    assert got.shape == (24, 16, 2) and np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+    w = [rng.standard_normal((16, 12, 8)).astype(np.float32) for _ in range(4)]
+    got = F.physical_to_spectral(tuple(w), spectral=F.GB300Spectral(32))
+    ref = np.stack([np.fft.fftn(x.astype(np.float64)) for x in w], axis=-1) / w[0].size
+    assert got.shape == (16, 12, 8, 4) and got.dtype == np.complex64
+    assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max()
