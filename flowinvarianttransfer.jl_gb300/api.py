@@ -45,6 +45,10 @@ def _ft(arr):
 
 
 def _plan(velocity_hat, ks, dealiasing, spectral, advecting_hat):
+    if isinstance(spectral, DirectSumBackend) and isinstance(dealiasing, PaddedThreeHalves):
+        # the reference's dependency-free backend rejects the exact 3/2 rule (src/NonlinearTerm.jl:106-109)
+        raise ValueError("PaddedThreeHalves dealiasing requires the FFT path — pass spectral=FFTBackend() (or "
+                         "GB300Spectral()). DirectSumBackend supports only NoDealiasing/OrszagTwoThirds.")
     nd = len(ks)
     v = np.asarray(velocity_hat)
     ns = v.shape[:nd]

@@ -64,3 +64,16 @@ def test_physical_stack_arguments():
         _physical_stack(np.zeros((2, 2, 2, 2)))
     with pytest.raises(ValueError):
         _physical_stack(())
+
+
+def test_direct_sum_rejects_three_halves():
+    """DirectSumBackend with the exact 3/2 rule is an ArgumentError-class error, as in the reference
+    (src/NonlinearTerm.jl:106-109, test/runtests.jl:341-343); raised before any device work."""
+    import numpy as np
+    import pytest
+    ks = F.wavenumber_grid((8, 8), (2 * np.pi, 2 * np.pi))
+    u = np.zeros((8, 8, 2), dtype=np.complex128)
+    with pytest.raises(ValueError, match="PaddedThreeHalves"):
+        F.compute_nonlinear_term(u, ks, dealiasing=F.PaddedThreeHalves(), spectral=F.DirectSumBackend())
+    with pytest.raises(ValueError, match="PaddedThreeHalves"):
+        F.calculate_spectral_flux(u, ks, dealiasing=F.PaddedThreeHalves(), spectral=F.DirectSumBackend())
