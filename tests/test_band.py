@@ -97,7 +97,7 @@ def test_band_3d_live_box_fp32(deal, inv, adv):
 
 @pytest.mark.gpu
 def test_band_live_box_many_bands_match_plain_path():
-    """12 bands (two binning passes of at most 8 carrier sets each) on the live box against the
+    """12 bands (two band-binning launches of at most 8 bands each) on the live box against the
     plan's FP64 path on the same 64^3 field."""
     u, ks = curl_noise_3d(64, 5)
     centers = list(np.geomspace(1.0, 24.0, 12))
