@@ -102,3 +102,18 @@ def test_single_rank_replica_arithmetic():
     assert bench.allmax(1, 3.5) == 3.5
     value, ms = bench.replica_throughput(1, 1.0, 91.5)
     assert ms == 91.5 and value == pytest.approx(1000.0 / 91.5)
+
+
+def test_default_arguments_meet_the_contract(monkeypatch):
+    """No flags: one GPU, the 512^3 headline configuration, at least 3 warm-up steps, our arm; every
+    config the dispatcher knows is accepted by the parser."""
+    import sys
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    a = bench.parse()
+    assert a.gpus == 1 and a.config == "s2s" and a.impl == "ours" and a.n == 512
+    assert a.warmup >= 3 and a.steps >= 1
+    src = open(os.path.join(bench.ROOT, "bench.py")).read()
+    import re
+    for cfg in re.findall(r'args\.config == "([a-z0-9]+)"', src):
+        monkeypatch.setattr(sys, "argv", ["bench.py", "--config", cfg])
+        assert bench.parse().config == cfg
