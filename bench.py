@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--oracle-column", type=int, default=8,
+                    help="1-based mediator shell whose full column the oracle computes for the headline's "
+                         "error line (0: skip)")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison")
     ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial", "padded", "m2m", "band", "frontend"],
                     help="s2s: the 512^3 shell-to-shell headline; closure: learned closure vs exact "
@@ -274,7 +277,21 @@ def cpu_sample(u_np, ks, dk, reps=1):
         times.append(time.perf_counter() - t0)
     t_piece = float(np.mean(times))
     t_matrix = t_setup + nsh * 3 * t_piece
-    return t_setup, t_piece, t_matrix, cores, nsh
+    return t_setup, t_piece, t_matrix, cores, nsh, st
+
+
+def julia_probe():
+    """Whether a Julia toolchain exists on this host (the reference's own CPU path needs one, plus
+    FlowInvariantTransfer.jl and FFTW.jl installed for it)."""
+    import shutil
+    exe = shutil.which("julia")
+    if not exe:
+        return {"found": False}
+    try:
+        v = subprocess.run([exe, "--version"], capture_output=True, text=True, timeout=60).stdout.strip()
+    except Exception as e:
+        v = f"failed: {e}"
+    return {"found": True, "path": exe, "version": v}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -318,8 +335,9 @@ def run_reference(args):
                        "seed": args.seed},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference is Julia (FFTW+OhMyThreads); no Julia toolchain exists on this box, so the "
-                    "timed CPU implementation is the FP64 oracle restatement of its algorithm"}
+            "julia": julia_probe(),
+            "note": "the reference is Julia (FFTW+OhMyThreads) and is not installed on this box, so the timed "
+                    "CPU implementation is the FP64 oracle restatement of its algorithm"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -442,6 +460,8 @@ def run_ours(args):
 
     # ---- plain FP64 form (one nonlinear term per mediator) ----
     fp64 = None
+    T64n = None
+    oracle_col = None
     if not args.no_fp64:
         del plan
         F.clear_plans()
@@ -480,11 +500,25 @@ def run_ours(args):
             import oracle as O
             u_np = host_field(u)
             ksd = O.wavenumber_grid(ns, (2 * np.pi,) * 3)
-            t_setup, t_piece, t_matrix, cores, _ = cpu_sample(u_np, ksd, args.dk)
+            t_setup, t_piece, t_matrix, cores, _, st = cpu_sample(u_np, ksd, args.dk)
             cpu = {"value": 1.0 / t_matrix, "unit": UNIT, "cores": cores, "kind": "port",
                    "sample": f"oracle restatement (FP64, scipy.fft x{cores} threads) of the same 512^3 field: "
                              f"setup {t_setup:.1f} s + one advected component of one mediator {t_piece:.1f} s; "
                              f"T(n,m) = setup + {nsh}x3 pieces"}
+            if args.oracle_column >= 1:
+                # one full column of the headline matrix from the oracle: the FP32 and FP64 GPU
+                # results against the FFT-based FP64 restatement of the reference on the same field
+                m = args.oracle_column - 1
+                t0 = time.perf_counter()
+                col = O.s2s_column(st, m)
+                # errors in max-norm relative to max|T| over the whole matrix
+                sc = float(np.max(np.abs(T64n if T64n is not None else T32)))
+                oracle_col = {"m": m + 1, "seconds": time.perf_counter() - t0,
+                              "max_abs_T_column": float(np.max(np.abs(col))), "max_abs_T": sc,
+                              "rel_err_fp32_maxnorm": float(np.max(np.abs(T32.T[:, m] - col)) / sc)}
+                if T64n is not None:
+                    oracle_col["rel_err_fp64_maxnorm"] = float(np.max(np.abs(T64n.T[:, m] - col)) / sc)
+            del st
         except Exception as e:   # the baseline never blocks the GPU line
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
 
@@ -499,7 +533,7 @@ def run_ours(args):
                            "l2": "inputs 3.2 GB per step >> 129 MB L2; no flush needed"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches / args.steps),
                 "gpu_launches_timed_region": int(launches), "clocks": clocks, "fp64_plain": fp64,
-                "cufft_comparison": cufft}
+                "oracle_column": oracle_col, "cufft_comparison": cufft}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -633,6 +667,42 @@ def make_field_nd(ns, seed, device, spectrum, ncomp=None, project=True, dtype=No
     return u.to(dtype or torch.complex64).contiguous()
 
 
+def draw_batch_instances(F, seed, n_instances, dev):
+    """The uneven batch drawn from ``seed``: instance i is 2D (64^2..1024^2) when i % 4 < 2, else 3D
+    (64^3..192^3), sizes 2^n and 3*2^n; odd instances carry a passive scalar; shell geometry drawn
+    from isotropic / perpendicular / parallel. Returns the FP32 and FP64 instance specs (device
+    fields), a description per instance and the FP32 input bytes."""
+    import torch
+    rng = np.random.default_rng(seed)
+    sizes2 = [64, 96, 128, 192, 256, 384, 512, 768, 1024]
+    sizes3 = [64, 96, 128, 192]
+    e_vel = lambda k: k ** 4 * torch.exp(-2 * (k / 4) ** 2)          # noqa: E731
+    e_sca = lambda k: k ** 2 * torch.exp(-(k / 6) ** 2)              # noqa: E731
+    geos = ["isotropic", "perpendicular", "parallel"]
+    specs32, specs64, desc = [], [], []
+    h2d = 0
+    for i in range(n_instances):
+        nd = 2 if i % 4 < 2 else 3
+        n = int(rng.choice(sizes2 if nd == 2 else sizes3))
+        ns = (n,) * nd
+        ks = F.wavenumber_grid(ns, (2 * np.pi,) * nd)
+        scalar = i % 2 == 1
+        gname = geos[int(rng.integers(0, 3))]
+        geo = {"isotropic": F.IsotropicShells(), "perpendicular": F.PerpendicularShells(),
+               "parallel": F.ParallelShells(dims=(nd,))}[gname]
+        u = make_field_nd(ns, seed * 1000 + 2 * i, dev, e_vel, dtype=torch.complex128)
+        th = make_field_nd(ns, seed * 1000 + 2 * i + 1, dev, e_sca, ncomp=1, project=False,
+                           dtype=torch.complex128) if scalar else None
+        base = {"ks": ks, "ns": ns, "geometry": geo, "binning": F.LinearBinning(1.0)}
+        specs64.append(dict(base, velocity_dev=u.view(-1), scalar_dev=th.view(-1) if scalar else None))
+        u32 = u.to(torch.complex64).view(-1)
+        th32 = th.to(torch.complex64).view(-1) if scalar else None
+        specs32.append(dict(base, velocity_dev=u32, scalar_dev=th32))
+        h2d += u32.numel() * 8 + (th32.numel() * 8 if scalar else 0)
+        desc.append(f"{'x'.join(map(str, ns))}:{'scalar' if scalar else 'ke'}:{gname}")
+    return specs32, specs64, desc, h2d
+
+
 def run_batch(args):
     """64 uneven spectral-flux instances (half kinetic energy, half passive scalar; 2D 64^2..1024^2 and
     3D 64^3..192^3, sizes 2^n and 3*2^n; isotropic / perpendicular / parallel shells) as ONE graph
@@ -642,33 +712,7 @@ def run_batch(args):
     F = __graft_entry__.load_package()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    rng = np.random.default_rng(args.seed)
-    sizes2 = [64, 96, 128, 192, 256, 384, 512, 768, 1024]
-    sizes3 = [64, 96, 128, 192]
-    e_vel = lambda k: k ** 4 * torch.exp(-2 * (k / 4) ** 2)          # noqa: E731
-    e_sca = lambda k: k ** 2 * torch.exp(-(k / 6) ** 2)              # noqa: E731
-    geos = ["isotropic", "perpendicular", "parallel"]
-    specs32, specs64, desc = [], [], []
-    h2d = 0
-    for i in range(args.instances):
-        nd = 2 if i % 4 < 2 else 3
-        n = int(rng.choice(sizes2 if nd == 2 else sizes3))
-        ns = (n,) * nd
-        ks = F.wavenumber_grid(ns, (2 * np.pi,) * nd)
-        scalar = i % 2 == 1
-        gname = geos[int(rng.integers(0, 3))]
-        geo = {"isotropic": F.IsotropicShells(), "perpendicular": F.PerpendicularShells(),
-               "parallel": F.ParallelShells(dims=(nd,))}[gname]
-        u = make_field_nd(ns, args.seed * 1000 + 2 * i, dev, e_vel, dtype=torch.complex128)
-        th = make_field_nd(ns, args.seed * 1000 + 2 * i + 1, dev, e_sca, ncomp=1, project=False,
-                           dtype=torch.complex128) if scalar else None
-        base = {"ks": ks, "ns": ns, "geometry": geo, "binning": F.LinearBinning(1.0)}
-        specs64.append(dict(base, velocity_dev=u.view(-1), scalar_dev=th.view(-1) if scalar else None))
-        u32 = u.to(torch.complex64).view(-1)
-        th32 = th.to(torch.complex64).view(-1) if scalar else None
-        specs32.append(dict(base, velocity_dev=u32, scalar_dev=th32))
-        h2d += u32.numel() * 8 + (th32.numel() * 8 if scalar else 0)
-        desc.append(f"{'x'.join(map(str, ns))}:{'scalar' if scalar else 'ke'}:{gname}")
+    specs32, specs64, desc, h2d = draw_batch_instances(F, args.seed, args.instances, dev)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -781,9 +825,9 @@ def run_batch(args):
 
 def run_partial(args):
     """512^3 helical partial fluxes Pi^{s_k s_p s_q}(K) of kinetic energy AND helicity (2 x 8 channels,
-    DyadicBinning(1), 2/3 rule) from one pass (four shared nonlinear terms), replayed as one CUDA
-    graph: FP32 transforms and products, FP64 shell sums. Compared with the per-invariant plain
-    path in FP32 and in FP64 (the error reference)."""
+    DyadicBinning(2): 8 bands [2,4)..[256,512), 2/3 rule) from one pass (four shared nonlinear
+    terms), replayed as one CUDA graph: FP32 transforms and products, FP64 shell sums. Compared with
+    the per-invariant plain path in FP32 and in FP64 (the error reference)."""
     import torch
     import __graft_entry__
     F = __graft_entry__.load_package()
@@ -792,7 +836,7 @@ def run_partial(args):
     N = args.n
     ns = (N, N, N)
     ks = F.wavenumber_grid(ns, (2 * np.pi,) * 3)
-    edges = np.asarray(F.shell_edges(F.DyadicBinning(1.0), F.kmax(ks)), dtype=np.float64)
+    edges = np.asarray(F.shell_edges(F.DyadicBinning(2.0), F.kmax(ks)), dtype=np.float64)
     nsh = len(edges) - 1
     u = make_field(N, args.seed, dev)
     stream = torch.cuda.Stream(device=dev)
@@ -876,7 +920,7 @@ def run_partial(args):
             "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{N}^3 D=3 {dname_} 8 channels x (KineticEnergy, Helicity), "
-                                   f"DyadicBinning(1) ({nsh} bands), OrszagTwoThirds, complex64 fields, FP64 sums",
+                                   f"DyadicBinning(2) ({nsh} bands), OrszagTwoThirds, complex64 fields, FP64 sums",
                        "spectrum": "k^-5/3 on [4,170], k^4 rise below 4, solenoidal", "seed": args.seed,
                        "l2": "inputs 3.2 GB per step >> 129 MB L2"},
             "roofline": roofline, "ms_plain_fp32_two_calls": ms_plain32, "speedup_vs_plain_fp32": ms_plain32 / ms,

@@ -19,6 +19,7 @@ EXPORTS = [
     "fit_batch_create", "fit_batch_destroy", "fit_batch_add_flux", "fit_batch_run", "fit_batch_run_eager", "fit_batch_info",
     "fit_autotune_enable", "fit_autotune_clear", "fit_autotune_info", "fit_autotune_entry",
     "fit_partial_fluxes_batched", "fit_band_to_band", "fit_stress_residual",
+    "fit_set_shell_index", "fit_shell_to_shell_indexed",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -48,6 +49,8 @@ def _declare(lib):
     lib.fit_transfer_density.argtypes = [vp, i32, vp, vp, vp, i32]
     lib.fit_spectral_flux.argtypes = [vp, vp, vp, vp, dp, i32, u32, i32, i32, vp, vp, i32]
     lib.fit_shell_to_shell.argtypes = [vp, vp, vp, dp, i32, u32, i32, i32, i32, i32, vp, vp, vp, i32]
+    lib.fit_set_shell_index.argtypes = [vp, vp, i32, i32]
+    lib.fit_shell_to_shell_indexed.argtypes = [vp, vp, vp, i32, i32, i32, vp, vp, vp, i32]
     lib.fit_helical_decompose.argtypes = [vp, vp, vp, vp, i32]
     lib.fit_toroidal_poloidal_decompose.argtypes = [vp, vp, vp, vp, i32]
     lib.fit_helmholtz_decompose.argtypes = [vp, vp, vp, vp, i32]

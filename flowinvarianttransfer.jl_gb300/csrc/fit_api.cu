@@ -7,6 +7,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "fit_gb300.h"
@@ -73,6 +74,15 @@ const char* fit_get_error() { return g_err; }
 void fit_count_launches(long n) { g_launches += n; }
 long fit_launch_total() { return (long)g_launches.load(); }
 
+long long fit_wait_cycles() {
+  const char* v = getenv("FIT_TEST_WAIT_CYCLES");
+  if (v && v[0]) {
+    const long long c = atoll(v);
+    if (c > 0) return c;
+  }
+  return FIT_WAIT_CYCLES;
+}
+
 #define API_CHECK(cond, code, ...)  \
   do {                              \
     if (!(cond)) {                  \
@@ -131,6 +141,8 @@ int ensure_shells(fit_plan* p, const double* edges, int n_edges, unsigned dims, 
   p->cached_dims = dims;
   p->cached_f32 = coord_f32;
   p->nsh = n_edges - 1;
+  p->shell_gen++;
+  std::vector<uint16_t>().swap(p->idx_host);
   return FIT_OK;
 }
 
@@ -434,7 +446,8 @@ int fit_plan_destroy(fit_plan* p) {
   s2s_free(p);
   partial_free(p);
   fit_dbuf* bufs[] = {&p->in_u, &p->in_a, &p->in_c, &p->out_c, &p->out_c2, &p->hs, &p->ph, &p->nph, &p->nh,
-                      &p->ceff, &p->seff, &p->partial, &p->outd, &p->shell_full, &p->edges_dev, &p->wtab};
+                      &p->ceff, &p->seff, &p->partial, &p->outd, &p->shell_full, &p->edges_dev, &p->wtab,
+                      &p->flag};
   for (fit_dbuf* b : bufs) release(b);
   for (int d = 0; d < 3; ++d) {
     if (p->ax_init[d]) axis_free(&p->ax[d]);
@@ -572,26 +585,30 @@ int fit_spectral_flux(fit_plan* p, const void* u_hat, const void* adv_hat, const
   return FIT_OK;
 }
 
-int fit_shell_to_shell(fit_plan* p, const void* u_hat, const void* adv_hat, const double* edges, int n_edges,
-                       uint32_t dims_mask, int coord_f32, int invariant, int mode, int verify, double* T_colmajor,
-                       double* net, double* max_asym, int ptr_kind) {
-  API_CHECK(p != nullptr && u_hat != nullptr && T_colmajor != nullptr, FIT_ERR_ARG, "NULL argument");
+// Inputs of a shell-to-shell call on the device (the batched form on a 2/3 plan copies only the
+// kept box of host inputs).
+static int s2s_stage(fit_plan* p, const void* u_hat, const void* adv_hat, int invariant, int mode, int ptr_kind,
+                     const void** ud, const void** ad) {
   FIT_TRY(check_invariant(p, invariant, p->M));
   API_CHECK(mode == FIT_S2S_PLAIN || mode == FIT_S2S_BATCHED, FIT_ERR_ARG, "unknown shell-to-shell mode %d", mode);
   const size_t fb = cbytes(p) * p->g.Ntot * p->M, ab = cbytes(p) * p->g.Ntot * p->Dadv;
-  const void *ud, *ad;
   if (mode == FIT_S2S_BATCHED && ptr_kind != FIT_PTR_DEVICE && s2s_reads_kept_box(p)) {
-    FIT_TRY(stage_in_kept_box(p, &p->in_u, u_hat, fb, p->M, &ud));
-    FIT_TRY(stage_in_kept_box(p, &p->in_a, adv_hat, ab, p->Dadv, &ad));
+    FIT_TRY(stage_in_kept_box(p, &p->in_u, u_hat, fb, p->M, ud));
+    FIT_TRY(stage_in_kept_box(p, &p->in_a, adv_hat, ab, p->Dadv, ad));
   } else {
-    FIT_TRY(stage_in(p, &p->in_u, u_hat, fb, ptr_kind, &ud));
-    FIT_TRY(stage_in(p, &p->in_a, adv_hat, ab, ptr_kind, &ad));
+    FIT_TRY(stage_in(p, &p->in_u, u_hat, fb, ptr_kind, ud));
+    FIT_TRY(stage_in(p, &p->in_a, adv_hat, ab, ptr_kind, ad));
   }
-  if (!ad) {
+  if (!*ad) {
     API_CHECK(p->M >= p->nd, FIT_ERR_ARG, "self-advection needs >= nd components (pass advecting_hat)");
-    ad = ud;
+    *ad = *ud;
   }
-  FIT_TRY(ensure_shells(p, edges, n_edges, dims_mask, coord_f32));
+  return FIT_OK;
+}
+
+// T(n,m), net and max|T+T'| once the inputs are staged and the plan's shell table is set.
+static int s2s_run(fit_plan* p, const void* ud, const void* ad, int invariant, int mode, int verify,
+                   double* T_colmajor, double* net, double* max_asym, int ptr_kind) {
   const int nsh = p->nsh;
   FIT_TRY(ensure(p, &p->outd, sizeof(double) * (size_t)nsh * nsh));
   double* Td = (double*)p->outd.p;
@@ -636,6 +653,115 @@ int fit_shell_to_shell(fit_plan* p, const void* u_hat, const void* adv_hat, cons
   if (net) memcpy(net, nt.data(), sizeof(double) * nsh);
   if (max_asym) *max_asym = asym;
   return FIT_OK;
+}
+
+int fit_shell_to_shell(fit_plan* p, const void* u_hat, const void* adv_hat, const double* edges, int n_edges,
+                       uint32_t dims_mask, int coord_f32, int invariant, int mode, int verify, double* T_colmajor,
+                       double* net, double* max_asym, int ptr_kind) {
+  API_CHECK(p != nullptr && u_hat != nullptr && T_colmajor != nullptr, FIT_ERR_ARG, "NULL argument");
+  const void *ud, *ad;
+  FIT_TRY(s2s_stage(p, u_hat, adv_hat, invariant, mode, ptr_kind, &ud, &ad));
+  FIT_TRY(ensure_shells(p, edges, n_edges, dims_mask, coord_f32));
+  return s2s_run(p, ud, ad, invariant, mode, verify, T_colmajor, net, max_asym, ptr_kind);
+}
+
+// Host shell index -> uint16 table, validated, split over up to 32 threads; *same tells whether the
+// table equals prev (NULL: no previous table). Returns the lowest bad position, or -1.
+static long index_to_table(const int64_t* idx, long n, int nsh, uint16_t* out, const uint16_t* prev, bool* same) {
+  const long cores = (long)std::thread::hardware_concurrency();
+  const int nthr = (int)(n < (1L << 20) ? 1 : (cores < 1 ? 1 : (cores > 32 ? 32 : cores)));
+  std::vector<long> bad((size_t)nthr, -1);
+  std::vector<char> eq((size_t)nthr, prev != nullptr);
+  auto work = [&](int t) {
+    const long a = n * t / nthr, b = n * (t + 1) / nthr;
+    bool e = prev != nullptr;
+    for (long i = a; i < b; ++i) {
+      const int64_t v = idx[i];
+      if (v < 0 || v > nsh) {
+        bad[(size_t)t] = i;
+        return;
+      }
+      out[i] = (uint16_t)v;
+      e = e && prev[i] == out[i];
+    }
+    eq[(size_t)t] = e;
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthr; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+  *same = prev != nullptr;
+  for (int t = 0; t < nthr; ++t) {
+    if (bad[(size_t)t] >= 0) return bad[(size_t)t];
+    *same = *same && eq[(size_t)t];
+  }
+  return -1;
+}
+
+// Installs a caller's shell index. A call whose index equals the installed one changes nothing, so
+// a caller that rebuilds the same index on every call (the reference makes a new workspace per
+// call) keeps the batched form's captured graph.
+int fit_set_shell_index(fit_plan* p, const int64_t* shell_idx, int n_shells, int ptr_kind) {
+  API_CHECK(p != nullptr && shell_idx != nullptr, FIT_ERR_ARG, "NULL argument");
+  API_CHECK(n_shells >= 1 && n_shells <= 65535, FIT_ERR_ARG, "n_shells must be in 1..65535 (got %d)", n_shells);
+  const long n = p->g.Ntot;
+  const bool installed = p->cached_f32 == -2 && p->nsh == n_shells && p->shell_full.p != nullptr;
+  bool changed = true;
+  if (ptr_kind == FIT_PTR_DEVICE) {
+    FIT_TRY(ensure(p, &p->shell_full, sizeof(uint16_t) * n));
+    FIT_TRY(ensure(p, &p->flag, 16));
+    FIT_CUDA_CHECK(cudaMemsetAsync(p->flag.p, 0xff, sizeof(unsigned long long), p->stream));
+    FIT_CUDA_CHECK(cudaMemsetAsync((char*)p->flag.p + 8, 0, sizeof(unsigned), p->stream));
+    FIT_TRY(shell_table_from_i64(p->g, shell_idx, n_shells, (uint16_t*)p->shell_full.p,
+                                 (unsigned long long*)p->flag.p, (unsigned*)((char*)p->flag.p + 8), p->stream));
+    unsigned long long h[2] = {0, 0};
+    FIT_CUDA_CHECK(cudaMemcpyAsync(h, p->flag.p, 16, cudaMemcpyDeviceToHost, p->stream));
+    FIT_TRY(sync_plan(p));
+    p->idx_host.clear();
+    if (h[0] != ~0ull) {
+      p->cached_edges.clear();   // the table is partly written: no cache key may match it
+      p->cached_f32 = -3;
+      p->shell_gen++;
+      fit_set_error("shell index at linear position %llu is outside [0, %d]", h[0], n_shells);
+      return FIT_ERR_ARG;
+    }
+    changed = (unsigned)h[1] != 0u;
+  } else {
+    std::vector<uint16_t> t((size_t)n);
+    bool same = false;
+    const long bad = index_to_table(shell_idx, n, n_shells, t.data(),
+                                    installed && p->idx_host.size() == (size_t)n ? p->idx_host.data() : nullptr,
+                                    &same);
+    API_CHECK(bad < 0, FIT_ERR_ARG, "shell index %lld at linear position %ld is outside [0, %d]",
+              (long long)shell_idx[bad < 0 ? 0 : bad], bad, n_shells);
+    if (same) {
+      changed = false;
+    } else {
+      FIT_TRY(ensure(p, &p->shell_full, sizeof(uint16_t) * n));
+      FIT_CUDA_CHECK(cudaMemcpyAsync(p->shell_full.p, t.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice,
+                                     p->stream));
+      FIT_TRY(sync_plan(p));
+      p->idx_host.swap(t);
+    }
+  }
+  if (installed && !changed) return FIT_OK;
+  p->cached_edges.clear();
+  p->cached_dims = 0;
+  p->cached_f32 = -2;
+  p->nsh = n_shells;
+  p->shell_gen++;
+  return FIT_OK;
+}
+
+int fit_shell_to_shell_indexed(fit_plan* p, const void* u_hat, const void* adv_hat, int invariant, int mode,
+                               int verify, double* T_colmajor, double* net, double* max_asym, int ptr_kind) {
+  API_CHECK(p != nullptr && u_hat != nullptr && T_colmajor != nullptr, FIT_ERR_ARG, "NULL argument");
+  API_CHECK(p->cached_f32 == -2 && p->nsh > 0, FIT_ERR_STATE,
+            "no shell index is installed on this plan (fit_set_shell_index, or a later call with shell edges "
+            "replaced it)");
+  const void *ud, *ad;
+  FIT_TRY(s2s_stage(p, u_hat, adv_hat, invariant, mode, ptr_kind, &ud, &ad));
+  return s2s_run(p, ud, ad, invariant, mode, verify, T_colmajor, net, max_asym, ptr_kind);
 }
 
 int fit_helical_decompose(fit_plan* p, const void* u_hat, void* up, void* um, int ptr_kind) {

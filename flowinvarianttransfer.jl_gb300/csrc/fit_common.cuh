@@ -43,6 +43,17 @@ template <typename V, bool POS> FIT_HD V cmuli(V a) { return POS ? mkc<V>(-a.y, 
 void fit_set_error(const char* fmt, ...);
 const char* fit_get_error();
 
+// Clock bound of every wait on a bulk copy or a tensor-core commit inside a kernel (about 1 s at
+// 2 GHz); bounds below FIT_WAIT_POLL_MIN poll without suspending (fit_tma.cuh).
+#define FIT_WAIT_CYCLES 2000000000LL
+#define FIT_WAIT_POLL_MIN 4096LL
+// Bound passed to the kernels' first waits: FIT_WAIT_CYCLES, or the value of the environment
+// variable FIT_TEST_WAIT_CYCLES when it is set to a positive number. Tests set it to a few cycles
+// so that the waits run out and the error path (device flag -> host error code) is exercised with
+// copies and commits that still complete; it is read at every launch (graphs keep the value they
+// were captured with).
+long long fit_wait_cycles();
+
 // Every launch of a library kernel is counted (graph replays add the kernels they contain).
 void fit_count_launches(long n);
 long fit_launch_total();

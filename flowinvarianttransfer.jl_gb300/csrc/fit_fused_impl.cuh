@@ -57,6 +57,7 @@ struct FzArgs {
   // widx[b] (box layout [band][kz'][col], KY P1 floats per band) as it loads it
   const float* wbox;
   int widx[16];
+  long long wlim;   // first bound of the x pass's copy waits (fit_wait_cycles)
 };
 
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
@@ -310,6 +311,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
     bulk_g2s(stg, G + (gb + l0) * a.KX, bytes, &bar[0]);
   }
   float2 acc[EPT];
+  bool failed = false;   // a first wait ran out (the second, full-bound wait then succeeded)
   for (int t = 0; t < 9; ++t) {
     const int c = t / 3, j = t % 3, buf = t & 1;
     if (j == 0) {
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
       ua[r] = Uj[la * N + x];
       ub[r] = Uj[(la + 1) * N + x];
     }
-    const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL);
+    const bool ok = mbar_wait_or_flag(&bar[buf], (uint32_t)((t >> 1) & 1), a.wlim, failed);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         atomicExch(err, 1);
@@ -393,6 +395,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
       __syncthreads();
     }
   }
+  if (failed) atomicExch(err, 1);
 }
 
 // ---- xmix, register-accumulating form -------------------------------------------------------------
@@ -467,12 +470,16 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
     for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + urow(r) * TT::UP, U + (l0 + r) * N, (uint32_t)(N * 4), &bar[2]);
   }
   // Every thread waits on the copy barriers itself (the completed phase makes the bulk-copied data
-  // visible to it), so no block barrier is spent on the waits. A wait that runs out marks this
-  // thread failed and the block carries on with whatever the tile holds (indices never depend on
-  // data, so every access stays in bounds and every thread reaches the same barriers); the flag
-  // tells the host to discard the result. Thread 0 waits on every phase too and stops issuing
-  // copies once one of its own waits failed, so every later wait is bounded as well.
-  bool failed = false;
+  // visible to it), so no block barrier is spent on the waits. A first wait that runs out marks
+  // the launch failed (the flag tells the host to discard the result) and is followed by a second
+  // wait with the full bound, which keeps the barrier phases in step with the issued copies. When
+  // that one runs out as well the thread is "broken": the block carries on with whatever the tile
+  // holds (indices never depend on data, so every access stays in bounds and every thread reaches
+  // the same barriers). Thread 0 waits on every phase too and stops issuing copies once it is
+  // broken, so every later wait is bounded as well; it counts the phases it issued per barrier
+  // and, before the block exits, waits for the last one of each, so no copy is still landing.
+  bool failed = false, broken = false;
+  int issued0 = 1, issued1 = 0, issued2 = 1;   // phases issued on bars 0, 1, 2 (thread 0)
   float2 acc[MB][RL];
   for (int t = 0; t < 9; ++t) {
     const int c = t / 3, j = t % 3, buf = t & 1;
@@ -482,14 +489,16 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
 #pragma unroll
         for (int q = 0; q < RL; ++q) acc[i][q] = make_float2(0.f, 0.f);
     }
-    if (tid == 0 && t + 1 < 9 && !failed) {   // after a failed wait, issue nothing more
+    if (tid == 0 && t + 1 < 9 && !broken) {   // once broken, issue nothing more
       const int c1 = (t + 1) / 3, j1 = (t + 1) % 3, nb1 = (t + 1) & 1;
       const long gb = (((long)b * 3 + c1) * 3 + j1) * a.L;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[nb1], gbytes);
       bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KX, gbytes, &bar[nb1]);
+      if (nb1) ++issued1;
+      else ++issued0;
     }
-    if (!mbar_wait_bounded(&bar[buf], (uint32_t)((t >> 1) & 1), 2000000000LL)) failed = true;
+    if (!mbar_wait_or_flag(&bar[buf], (uint32_t)((t >> 1) & 1), a.wlim, failed)) broken = true;
     const float2* sg = stg + buf * SB;
     ct_fft_mapped_mid<float2, true, N, C, NT, EPT>(
         s, tw, tid,
@@ -507,7 +516,7 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           return make_float2(A.x - B.y, A.y + B.x);
         },
         [&]() -> bool {   // the velocity tile of this j must have landed before the last stage
-          if (!mbar_wait_bounded(&bar[2], (uint32_t)(t & 1), 2000000000LL)) failed = true;
+          if (!mbar_wait_or_flag(&bar[2], (uint32_t)(t & 1), a.wlim, failed)) broken = true;
           return true;
         },
         [&](int i, int q, int x, int col, float2 zv) {
@@ -515,13 +524,14 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           acc[i][q].y += us[(col + C) * TT::UP + x] * zv.y;
         });
     __syncthreads();   // s and the velocity tile are free
-    if (tid == 0 && t + 1 < 9 && !failed) {   // after a failed wait, issue nothing more
+    if (tid == 0 && t + 1 < 9 && !broken) {   // once broken, issue nothing more
       const int j1 = (t + 1) % 3;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
       const float* src = U + (long)j1 * Mtot + l0 * N;
       for (int r = 0; r < 2 * C; ++r)
         bulk_g2s(us + urow(r) * TT::UP, src + (long)r * N, (uint32_t)(N * 4), &bar[2]);
+      ++issued2;
     }
     if (j == 2) {
       ct_fft_mapped<float2, false, N, C, NT, EPT>(
@@ -544,10 +554,10 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
     }
   }
   if (failed) atomicExch(err, 1);
-  if (tid == 0) {   // no copy may still be landing when the block exits: final phases 4, 3, 8
-    mbar_wait_bounded(&bar[0], 0u, 200000000LL);
-    mbar_wait_bounded(&bar[1], 1u, 200000000LL);
-    mbar_wait_bounded(&bar[2], 0u, 200000000LL);
+  if (tid == 0) {   // no copy may still be landing when the block exits: the last issued phase of each
+    mbar_wait_bounded(&bar[0], (uint32_t)((issued0 - 1) & 1), FIT_WAIT_CYCLES / 10);
+    if (issued1 > 0) mbar_wait_bounded(&bar[1], (uint32_t)((issued1 - 1) & 1), FIT_WAIT_CYCLES / 10);
+    mbar_wait_bounded(&bar[2], (uint32_t)((issued2 - 1) & 1), FIT_WAIT_CYCLES / 10);
   }
 }
 
@@ -912,10 +922,12 @@ int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, cons
   const size_t smr = XR::OFF_G + 2 * (size_t)(2 * XR::C * a.KX) * 8;
   const char* env = getenv("FIT_XMIX_BULK");   // selects the previous form of the x pass
   bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
+  FzArgs aw = a;
+  aw.wlim = fit_wait_cycles();
   if constexpr (XR::OK) {
     if (reg) {
       FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
-      FzArgs ax = a;
+      FzArgs ax = aw;
       ax.xpair = fz_xpair(a.KX, XR::C);
       k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, G, U, out, tw, err);
     }
@@ -923,7 +935,7 @@ int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, cons
   if (reg) {
   } else if (bulk) {
     FIT_TRY(ct_prep_fused(k_fz_xmix_bulk<N>, smx, XT::NTHR));
-    k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(a, G, U, out, tw, err);
+    k_fz_xmix_bulk<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XT::C))), XT::NTHR, smx, st>>>(aw, G, U, out, tw, err);
   } else {
     FIT_TRY(ct_prep_fused(k_fz_xmix<N>, TT::SMEM, TT::NTHR));
     k_fz_xmix<N><<<dim3(a.nb, 1, (unsigned)((a.L + 2 * C - 1) / (2 * C))), TT::NTHR, TT::SMEM, st>>>(a, G, U, out,

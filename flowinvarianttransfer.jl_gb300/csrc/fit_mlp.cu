@@ -290,7 +290,8 @@ FIT_D void hidden_to_a(uint32_t tl, const float* b, __nv_bfloat16* A2, int row) 
 __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict__ Pm, const float* __restrict__ X,
                                                         long ld, long P, const float* __restrict__ in_scale,
                                                         const float* __restrict__ t_scale, float* __restrict__ Y,
-                                                        float* __restrict__ Pi, int homog, float clark, int* err) {
+                                                        float* __restrict__ Pi, int homog, float clark, int* err,
+                                                        long long wlim) {
   extern __shared__ __align__(128) unsigned char mlp_tc_raw[];
   MlpTcSmem& S = *reinterpret_cast<MlpTcSmem*>(mlp_tc_raw);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
   uint32_t phase = 0;
   bool failed = false;
   auto wait_mma = [&]() {
-    if (!mbar_wait_bounded(&S.bar, phase, 2000000000LL)) failed = true;
+    mbar_wait_or_flag(&S.bar, phase, wlim, failed);   // a second, full-bound wait keeps phases in step
     phase ^= 1u;
     tc_fence_after();
   };
@@ -452,7 +453,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(const float* __restrict
                                                          const float* __restrict__ T, long ld, long P, long Ptot,
                                                          const float* __restrict__ in_scale,
                                                          const float* __restrict__ t_scale, float* __restrict__ grad,
-                                                         double* __restrict__ loss, int homog, int* err) {
+                                                         double* __restrict__ loss, int homog, int* err,
+                                                         long long wlim) {
   extern __shared__ __align__(128) unsigned char mlp_tr_raw[];
   MlpTrainTcSmem& S = *reinterpret_cast<MlpTrainTcSmem*>(mlp_tr_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -510,7 +512,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(const float* __restrict
   uint32_t phase = 0;
   bool failed = false;
   auto wait_mma = [&]() {
-    if (!mbar_wait_bounded(&S.bar, phase, 2000000000LL)) failed = true;
+    mbar_wait_or_flag(&S.bar, phase, wlim, failed);   // a second, full-bound wait keeps phases in step
     phase ^= 1u;
     tc_fence_after();
   };
@@ -1091,7 +1093,8 @@ extern "C" int fit_mlp_forward(const float* params, const float* X, int64_t ld, 
   if (blocks > ntile) blocks = ntile;
   k_mlp_forward_tc<<<(unsigned)blocks, 128, sizeof(MlpTcSmem), st>>>(params, X, ld, P, in_scale, t_scale, Y, Pi,
                                                                     homogeneous,
-                                                                    (float)(clark_ell * clark_ell / 12.0), err);
+                                                                    (float)(clark_ell * clark_ell / 12.0), err,
+                                                                    fit_wait_cycles());
   FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
@@ -1120,7 +1123,8 @@ extern "C" int fit_mlp_train_grad(const float* params, const float* X, const flo
     const long ntile = (P + 127) / 128;
     const long blocks = ntile < nsm ? ntile : nsm;   // one CTA per SM (256 tensor-memory columns, ~117 KB)
     k_mlp_train_tc<<<(unsigned)blocks, 128, sizeof(MlpTrainTcSmem), st>>>(params, X, T, ld, P, Ptot, in_scale,
-                                                                           t_scale, grad, loss, homogeneous, err);
+                                                                           t_scale, grad, loss, homogeneous, err,
+                                                                           fit_wait_cycles());
     FIT_LAUNCH_CHECK();
     return FIT_OK;
   }

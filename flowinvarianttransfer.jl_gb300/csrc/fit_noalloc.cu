@@ -13,7 +13,10 @@
 // process exits. All calls share it, and it keeps the previous call's contents: every entry a
 // call reads is written earlier in the same call, so nothing needs clearing, but two calls that
 // overlap on the GPU (different streams, or different host threads) race on the same array.
-// Serialise calls per device.
+// Serialise calls per device. The array's device address is looked up once per device and kept
+// for the life of the process: after cudaDeviceReset (or anything else that destroys and
+// re-creates the device's primary context) the kept address is stale, so such a caller must not
+// use this entry point again in that process.
 #include <mutex>
 
 #include "fit_gb300.h"
@@ -30,6 +33,16 @@ namespace fit {
 int triad_run_scratch(const GridDesc& g, const KTab& kt, int M, int two_thirds, int io_f64, const void* u,
                       const void* adv, int inv, int fp64, void* scratch, int nchunk, double* S, double* net,
                       cudaStream_t st);
+}
+
+// 1 when p is device (or managed) memory: the kernels dereference every array argument on the GPU.
+static bool noalloc_is_device(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();   // clear the error the call records for an unknown pointer
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
 // Device address of the array, looked up once per device (with that device current). In host
@@ -86,6 +99,22 @@ extern "C" int fit_mode_to_mode_noalloc(int nd, const int64_t* ns, int n_advecte
     fit_set_error("self-advection needs >= nd components (pass adv_hat)");
     return FIT_ERR_ARG;
   }
+  // every array is read or written by the kernels: reject NULL tables and host memory up front,
+  // before anything is launched
+  for (int d = 0; d < nd; ++d) {
+    if (ks_dev[d] == nullptr || !noalloc_is_device(ks_dev[d])) {
+      fit_set_error("ks_dev[%d] must be a device pointer to the axis-%d wavenumbers", d, d);
+      return FIT_ERR_ARG;
+    }
+  }
+  const void* arrays[4] = {u_hat, adv_hat, S, net};
+  const char* names[4] = {"u_hat", "adv_hat", "S", "net"};
+  for (int i = 0; i < 4; ++i) {
+    if (arrays[i] != nullptr && !noalloc_is_device(arrays[i])) {
+      fit_set_error("%s must be a device pointer (device or managed memory)", names[i]);
+      return FIT_ERR_ARG;
+    }
+  }
   long nm = 1;
   for (int d = 0; d < nd; ++d) {
     if (ns[d] < 1) {
@@ -119,6 +148,9 @@ extern "C" int fit_mode_to_mode_noalloc(int nd, const int64_t* ns, int n_advecte
   FIT_TRY(fit::triad_run_scratch(g, kt, n_advected, dealias == 1, io_f64 ? 1 : 0, u_hat,
                                  adv_hat ? adv_hat : u_hat, invariant, fp64_products ? 1 : 0, scratch,
                                  FIT_NOALLOC_CHUNKS, S, net, st));
-  FIT_CUDA_CHECK(cudaStreamSynchronize(st));
+  // a stream that is being captured cannot be synchronised: then the call returns after enqueuing
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FIT_CUDA_CHECK(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusNone) FIT_CUDA_CHECK(cudaStreamSynchronize(st));
   return FIT_OK;
 }

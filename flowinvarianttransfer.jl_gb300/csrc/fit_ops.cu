@@ -464,6 +464,27 @@ int shell_table_i64(const GridDesc& g, const uint16_t* sh, int64_t* out, cudaStr
   return FIT_OK;
 }
 
+__global__ void k_sh_from_i64(const int64_t* __restrict__ idx, long n, int nsh, uint16_t* __restrict__ out,
+                              unsigned long long* bad, unsigned* changed) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t v = idx[i];
+  const bool ok = v >= 0 && v <= nsh;
+  const uint16_t t = ok ? (uint16_t)v : (uint16_t)0;
+  if (out[i] != t) {
+    out[i] = t;
+    *changed = 1u;
+  }
+  if (!ok) atomicMin(bad, (unsigned long long)i);
+}
+
+int shell_table_from_i64(const GridDesc& g, const int64_t* idx, int nsh, uint16_t* out, unsigned long long* bad,
+                         unsigned* changed, cudaStream_t st) {
+  k_sh_from_i64<<<nblk(g.Ntot, 256), 256, 0, st>>>(idx, g.Ntot, nsh, out, bad, changed);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 // ---- per-mode density on the full grid ---------------------------------------------------------
 
 __global__ void k_density_full(GridDesc g, KTab kt, const void* car, const void* nhat, int f64, int nc, int inv,

@@ -148,6 +148,11 @@ int scatter_full(const GridDesc& g, const typename Vec2<T>::t* half, int nf, int
 int shell_table(const GridDesc& g, const KTab& kt, unsigned dims_mask, const double* edges, int nedges,
                 int coord_f32, uint16_t* out, cudaStream_t st);
 int shell_table_i64(const GridDesc& g, const uint16_t* sh, int64_t* out, cudaStream_t st);
+// A caller's shell index (Int64, 1-based, 0 = none; device memory) as the uint16 table, written over
+// the current one: the lowest position of an entry outside [0, nsh] goes to *bad (which must hold ~0
+// beforehand) and *changed is set to 1 when any entry differs from the table it replaces.
+int shell_table_from_i64(const GridDesc& g, const int64_t* idx, int nsh, uint16_t* out, unsigned long long* bad,
+                         unsigned* changed, cudaStream_t st);
 
 // Per-mode transfer density on the full N grid: t(k) = sum_c Re(conj(C_c(k)) N_c(k)).
 int density_full(const GridDesc& g, const KTab& kt, const void* carrier, const void* nhat, int in_f64,

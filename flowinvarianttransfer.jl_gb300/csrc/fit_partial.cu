@@ -46,6 +46,7 @@ struct PartialState {
   int key_f32 = -1;
   double* key_T = nullptr;
   long key_gen = -1;
+  long key_sgen = -1;
   cudaStream_t key_stream = nullptr;
 };
 
@@ -226,7 +227,7 @@ static int partial_batched(fit_plan* p, const void* ud, int dec, const int* invs
   std::vector<int> iv(invs, invs + ninv);
   const bool same = s->key_u == ud && s->key_decomp == dec && s->key_inv == iv && s->key_edges == p->cached_edges &&
                     s->key_dims == p->cached_dims && s->key_f32 == p->cached_f32 && s->key_T == Td &&
-                    s->key_gen == p->buf_gen && s->key_stream == p->stream;
+                    s->key_gen == p->buf_gen && s->key_stream == p->stream && s->key_sgen == p->shell_gen;
   if (!same) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
     s->exec = nullptr;
@@ -240,6 +241,7 @@ static int partial_batched(fit_plan* p, const void* ud, int dec, const int* invs
     s->key_T = Td;
     s->key_gen = p->buf_gen;
     s->key_stream = p->stream;
+    s->key_sgen = p->shell_gen;
     return FIT_OK;
   }
   // eager when profiling (per-launch events) or on the legacy default stream (not capturable)

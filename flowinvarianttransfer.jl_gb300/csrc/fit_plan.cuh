@@ -37,11 +37,14 @@ struct fit_plan {
   fit_dbuf ceff, seff, partial, outd;
   // shell table cache
   fit_dbuf shell_full;
+  fit_dbuf flag;   // small device scratch for argument checks done on the device
+  std::vector<uint16_t> idx_host;   // host copy of a shell table installed from a caller's index
   fit_dbuf edges_dev;
   std::vector<double> cached_edges;
   unsigned cached_dims = 0;
-  int cached_f32 = -1;
+  int cached_f32 = -1;   // -2: the table was installed from a caller's shell index (fit_set_shell_index)
   int nsh = 0;
+  long shell_gen = 0;    // bumped whenever the shell table changes: graphs and mode lists key on it
   // batched shell-to-shell state (fit_s2s.cu)
   void* s2s = nullptr;
   // batched partial-flux state (fit_partial.cu)

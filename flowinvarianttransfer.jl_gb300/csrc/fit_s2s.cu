@@ -55,6 +55,8 @@ struct S2SState {
   unsigned zl_dims = 0;
   int zl_f32 = -1;
   int zl_nsh = -1;
+  long zl_sgen = -1;
+  long key_sgen = -1;
 };
 
 void s2s_free(fit_plan* p) {
@@ -459,7 +461,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   FIT_LAUNCH_CHECK();
   const int ntile = (int)npt;
   if (s->zl_edges != p->cached_edges || s->zl_dims != p->cached_dims || s->zl_f32 != p->cached_f32 ||
-      s->zl_nsh != nsh) {   // shell table changed: rebuild the z-pass mode lists (an eager call)
+      s->zl_nsh != nsh || s->zl_sgen != p->shell_gen) {   // shell table changed: rebuild the z-pass mode lists (an eager call)
     const long nmodes = nset, nl = (long)nsh * ntile;
     FIT_TRY(ensure(p, &s->zoff, sizeof(unsigned) * (size_t)(nl + 1)));
     FIT_TRY(ensure(p, &s->zfill, sizeof(unsigned) * (size_t)nl));
@@ -478,6 +480,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     s->zl_dims = p->cached_dims;
     s->zl_f32 = p->cached_f32;
     s->zl_nsh = nsh;
+    s->zl_sgen = p->shell_gen;
   }
   FzArgs a;
   memset(&a, 0, sizeof(a));
@@ -880,7 +883,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
   // output, the shell set and every workspace allocation are unchanged.
   const bool same = s->key_u == ud && s->key_a == ad && s->key_inv == inv && s->key_edges == p->cached_edges &&
                     s->key_dims == p->cached_dims && s->key_f32 == p->cached_f32 && s->key_T == Td &&
-                    s->key_gen == p->buf_gen;
+                    s->key_gen == p->buf_gen && s->key_sgen == p->shell_gen;
   if (!same) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
     s->exec = nullptr;
@@ -916,6 +919,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
     s->key_f32 = p->cached_f32;
     s->key_T = Td;
     s->key_gen = p->buf_gen;
+    s->key_sgen = p->shell_gen;
     return FIT_OK;
   }
   if (fit_prof_on()) {   // per-launch events need eager launches

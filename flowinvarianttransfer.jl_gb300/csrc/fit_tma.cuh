@@ -46,13 +46,43 @@ FIT_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait on phase `parity`: false after max_cycles SM clocks (about 1 s at 2 GHz for 2e9).
+// Non-blocking probe of phase `parity` (mbarrier.test_wait never suspends the thread).
+FIT_D bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on phase `parity`: false after max_cycles SM clocks (about 1 s at 2 GHz for the
+// default FIT_WAIT_CYCLES). try_wait may suspend the thread for a while inside one probe, so a
+// bound below FIT_WAIT_POLL_MIN cycles polls with the non-blocking test_wait instead: such a
+// short bound then runs out whenever the phase is still pending at the first probes.
 FIT_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long max_cycles) {
   const long long t0 = clock64();
+  if (max_cycles < FIT_WAIT_POLL_MIN) {
+    while (!mbar_test_wait(bar, parity)) {
+      if (clock64() - t0 > max_cycles) return false;
+    }
+    return true;
+  }
   while (!mbar_try_wait(bar, parity)) {
     if (clock64() - t0 > max_cycles) return false;
   }
   return true;
+}
+
+// Wait whose bound `lim` may run out: a wait that gives up marks `failed` (the launch's result is
+// then discarded by the host) and waits again on the same phase with the full bound, so that the
+// barrier's phases stay in step with the copies or tensor-core commits already issued. Returns
+// false only when that second wait gives up as well.
+FIT_D bool mbar_wait_or_flag(uint64_t* bar, uint32_t parity, long long lim, bool& failed) {
+  if (mbar_wait_bounded(bar, parity, lim)) return true;
+  failed = true;
+  return mbar_wait_bounded(bar, parity, FIT_WAIT_CYCLES);
 }
 
 }  // namespace fit

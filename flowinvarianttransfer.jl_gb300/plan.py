@@ -122,6 +122,29 @@ class Plan:
                                               self._vp(asym), PTR_HOST))
         return T, net, float(asym[0])
 
+    def set_shell_index(self, shell_idx, n_shells):
+        """Install a precomputed shell index (Int64, 1-based, 0 = none; the ``ws.shell_idx`` of the
+        reference's ShellToShellWorkspace) as this plan's shell table."""
+        idx = np.asarray(shell_idx)
+        if idx.shape != self.ns:
+            raise ValueError(f"shell index has shape {idx.shape}; expected {self.ns}")
+        idx = np.asfortranarray(idx.astype(np.int64, copy=False))
+        with self.lock:
+            check(self.lib.fit_set_shell_index(self.h, self._vp(idx), int(n_shells), PTR_HOST))
+
+    def shell_to_shell_indexed(self, u_hat, n_shells, inv, mode, verify=True, adv_hat=None):
+        """shell_to_shell binned by the index installed with set_shell_index."""
+        u = self._field(u_hat, self.M)
+        a = None if adv_hat is None else self._field(adv_hat, self.D)
+        n = int(n_shells)
+        T = np.zeros((n, n), order="F")
+        net = np.zeros(n)
+        asym = np.zeros(1)
+        with self.lock:
+            check(self.lib.fit_shell_to_shell_indexed(self.h, self._vp(u), self._vp(a), inv, mode, int(verify),
+                                                      self._vp(T), self._vp(net), self._vp(asym), PTR_HOST))
+        return T, net, float(asym[0])
+
     def band_to_band(self, u_hat, centers, logwidth, dmask, coord_f32, inv, adv_hat=None):
         u = self._field(u_hat, self.M)
         a = None if adv_hat is None else self._field(adv_hat, self.D)

@@ -114,6 +114,21 @@ int fit_shell_to_shell(fit_plan* plan, const void* u_hat, const void* adv_hat, c
                        uint32_t dims_mask, int coord_f32, int invariant, int mode, int verify, double* T_colmajor,
                        double* net, double* max_asym, int ptr_kind);
 
+/* Installs a caller's shell index as the plan's shell table: one Int64 per grid mode, column-major
+ * over ns, 1-based, 0 = no shell, exactly as assign_shells returns it and as
+ * ShellToShellWorkspace keeps it in ws.shell_idx (src/Workspaces.jl:154-169,
+ * src/ShellBinning.jl:126-140) for whatever shell geometry the workspace was built with.
+ * n_shells = length(edges) - 1. An entry outside [0, n_shells] returns FIT_ERR_ARG. The table
+ * stays installed until a call that passes shell edges replaces it. */
+int fit_set_shell_index(fit_plan* plan, const int64_t* shell_idx, int n_shells, int ptr_kind);
+
+/* fit_shell_to_shell binned by the installed shell index instead of edges: the mediator loop of
+ * ext/FlowInvariantTransferFFTWExt.jl:245-275 (src/ShellToShell/ShellToShellTransfer.jl:193-224),
+ * which restricts and bins by ws.shell_idx. FIT_ERR_STATE when no index is installed. Repeated
+ * calls with the same pointers replay the batched form's CUDA graph, as fit_shell_to_shell does. */
+int fit_shell_to_shell_indexed(fit_plan* plan, const void* u_hat, const void* adv_hat, int invariant, int mode,
+                               int verify, double* T_colmajor, double* net, double* max_asym, int ptr_kind);
+
 /* Helical (Craya-Herring) split u = u+ + u- (src/Decomposition.jl:63-98). */
 int fit_helical_decompose(fit_plan* plan, const void* u_hat, void* u_plus, void* u_minus, int ptr_kind);
 /* Rotational/divergent split of a 2D field (spectral Leray projection; the reference delegates
@@ -259,9 +274,14 @@ int fit_field_compare(const float* a, const float* b, int64_t P, double* out, vo
  * counterpart in the reference. Every array argument is a device pointer (ks_dev: nd device
  * arrays); no plan is used and nothing is allocated: intermediates live in one fixed 6.5 MiB
  * device array that each GPU loading the library holds until exit. Grids of at most 32768 modes
- * (32^3); larger grids return FIT_ERR_SIZE. The first call on a device looks up that array's
- * device address (do it before any stream capture). Calls share the array, so calls that
- * overlap on the GPU race: serialise them per device. stream may be NULL (default stream). */
+ * (32^3); larger grids return FIT_ERR_SIZE. Every array argument (ks_dev[d] included) must be
+ * device or managed memory: NULL tables and host pointers return FIT_ERR_ARG before anything is
+ * launched. The first call on a device looks up that array's device address (do it before any
+ * stream capture); the address is kept for the process, so the entry point must not be used again
+ * after cudaDeviceReset. Calls share the array, so calls that overlap on the GPU race: serialise
+ * them per device. The call synchronises `stream` before returning, except while that stream is
+ * being captured (it then returns once the work is enqueued). stream may be NULL (default
+ * stream). */
 int fit_mode_to_mode_noalloc(int nd, const int64_t* ns, int n_advected, int n_advecting, int dealias,
                              const double* const* ks_dev, int invariant, int fp64_products, int io_f64,
                              const void* u_hat, const void* adv_hat, double* S, double* net, void* stream);

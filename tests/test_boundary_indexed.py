@@ -1,0 +1,64 @@
+"""The call sequence of the Julia glue's shell-to-shell override, through the C ABI.
+
+The reference builds ``ws.shell_idx`` for the caller's shell geometry once per workspace
+(``src/Workspaces.jl:154-169``) and its mediator loop restricts and bins by it
+(``src/ShellToShell/ShellToShellTransfer.jl:193-224``, ``ext/FlowInvariantTransferFFTWExt.jl:245-275``).
+The glue keeps one plan per configuration in the workspace's plan bundle, installs that index with
+``fit_set_shell_index`` and calls ``fit_shell_to_shell_indexed`` on every call: the first call runs
+eagerly, the second captures the batched form's graph, later calls replay it. Here the same plan
+is reused for three calls per geometry (isotropic, perpendicular (1,2), parallel (3,)); each result
+matches the oracle: FP64 plain within 1e-11, FP32 batched within 1e-5 of max|T|. A call that bins by
+edges in between replaces the table, and the next indexed call reports it (the glue re-installs).
+"""
+import numpy as np
+import pytest
+
+import fit_gb300 as F
+import oracle as O
+from fields import curl_noise_3d, e_config2, spectrum_field
+from fit_gb300.plan import Plan
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dims", [None, (1, 2), (3,)])
+@pytest.mark.parametrize("form", ["fp64_plain", "fp32_batched"])
+def test_indexed_shell_to_shell_reused_plan(dims, form):
+    if form == "fp64_plain":
+        u, ks = curl_noise_3d(12, 3)
+        plan = Plan((12, 12, 12), 3, 3, "two_thirds", 64, True, ks)
+        mode, tol, binning = F._lib.S2S_PLAIN, 1e-11, ("linear", 2.0)
+    else:   # a fused transform size: the live-box pipeline with the caller's table
+        u, ks = spectrum_field((64, 64, 64), e_config2, seed=4)
+        plan = Plan((64, 64, 64), 3, 3, "two_thirds", 32, True, ks)
+        mode, tol, binning = F._lib.S2S_BATCHED, 1e-5, ("linear", 6.0)
+    _, edges, _, sidx = O.shell_setup(ks, binning, dims)
+    nsh = len(edges) - 1
+    _, _, Tref, netref, _ = O.shell_to_shell(u, ks, binning, "two_thirds", dims=dims)
+    scale = np.max(np.abs(Tref))
+    for _ in range(3):
+        # the reference builds a new workspace, and so a new index array, on every call: installing
+        # an index equal to the installed one keeps the plan's state (and its captured graph)
+        plan.set_shell_index(sidx.copy(), nsh)
+        T, net, asym = plan.shell_to_shell_indexed(u, nsh, 0, mode)
+        assert np.max(np.abs(T - Tref)) <= tol * scale
+        assert np.max(np.abs(net - netref)) <= 10 * tol * scale
+        assert asym == pytest.approx(np.max(np.abs(T + T.T)), rel=1e-12, abs=1e-300)
+    # an edges-based call replaces the plan's table: the indexed entry refuses until it is re-installed
+    plan.spectral_flux(u, edges, F.shells.dims_mask(F.IsotropicShells(), 3), 0, 0)
+    with pytest.raises(F.FitError, match="no shell index"):
+        plan.shell_to_shell_indexed(u, nsh, 0, mode)
+    plan.set_shell_index(sidx, nsh)
+    T, _, _ = plan.shell_to_shell_indexed(u, nsh, 0, mode)
+    assert np.max(np.abs(T - Tref)) <= tol * scale
+
+
+def test_set_shell_index_rejects_out_of_range():
+    u, ks = curl_noise_3d(8, 1)
+    plan = Plan((8, 8, 8), 3, 3, "two_thirds", 64, True, ks)
+    idx = np.ones((8, 8, 8), dtype=np.int64)
+    idx[3, 2, 1] = 5
+    with pytest.raises(ValueError, match="outside"):
+        plan.set_shell_index(idx, 4)
+    with pytest.raises(F.FitError, match="no shell index"):
+        plan.shell_to_shell_indexed(u, 4, 0, F._lib.S2S_PLAIN)
