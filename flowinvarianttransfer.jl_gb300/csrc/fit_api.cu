@@ -219,9 +219,11 @@ static int stage_in(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int
 }
 
 // Host inputs of a path that reads only the 2/3-kept modes: copy just the box of modes every axis
-// keeps (indices [0, K] and [N - K, N) per axis): per component, 8 pitched 3D copies (one per
-// octant of the box). Modes outside the box are left unwritten in the staging buffer and are
-// never read.
+// keeps (indices [0, K] and [N - K, N) per axis). Pinned host memory the device can address is read
+// by a kernel over the host link (one launch over the box's row runs; steadier and faster than the
+// copy engines on a coherent host link); other host memory goes through 8 pitched 3D copies per
+// component (one per octant of the box). Modes outside the box are left unwritten in the staging
+// buffer and are never read. FIT_KEPT_BOX_COPY_ENGINE=1 selects the 3D copies for pinned memory too.
 static int stage_in_kept_box(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int ncomp, const void** out) {
   if (src == nullptr) {
     *out = nullptr;
@@ -230,6 +232,19 @@ static int stage_in_kept_box(fit_plan* p, fit_dbuf* b, const void* src, size_t b
   FIT_TRY(ensure(p, b, bytes));
   const GridDesc& g = p->g;
   const size_t eb = cbytes(p), row = eb * g.N[0], plane = row * g.N[1];
+  cudaPointerAttributes at;
+  const char* env = getenv("FIT_KEPT_BOX_COPY_ENGINE");
+  const bool dma = env && env[0] == '1';
+  if (!dma && cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+      at.devicePointer != nullptr && ((uintptr_t)at.devicePointer % eb) == 0) {
+    FIT_TRY(copy_kept_box(at.devicePointer, b->p, g.N, ncomp, (int)eb, p->stream));
+    long kept = 1;
+    for (int d = 0; d < 3; ++d) kept *= 2L * (g.N[d] / 3 - 1) + 1;
+    p->h2d_total += (size_t)kept * ncomp * eb;
+    *out = b->p;
+    return FIT_OK;
+  }
+  cudaGetLastError();   // an unregistered pointer leaves an error from the attribute query
   int lo[3][2], n[3][2];
   for (int d = 0; d < 3; ++d) {
     const int K = g.N[d] / 3 - 1;   // kept iff min(k, N - k) < N / 3

@@ -360,33 +360,6 @@ struct CtXTile {
   static constexpr size_t SMEM = (size_t)(E + N) * VB;
 };
 
-// Twiddles w^(q*base) (conjugated for INV) of one radix-R butterfly, q = 1..R-1 (base*q < N). FP64:
-// one table load each. FP32: one table load of w = w^base and the powers as products, w^2 = w w,
-// w^3 = w^2 w, w^4 = w^2 w^2, w^5 = w^4 w, w^6 = w^4 w^2, w^7 = w^4 w^3 (at most three rounded
-// products deep: a few units in the last place of FP32), which saves R - 2 shared-memory loads per
-// butterfly in the FP32 transforms, whose stages are bound by shared-memory traffic.
-template <typename V, int R, bool INV>
-FIT_D void ct_twiddles(const V* tw, int base, V* w) {
-  if constexpr (sizeof(V) == 16) {
-#pragma unroll
-    for (int q = 1; q < R; ++q) {
-      V t = tw[base * q];
-      if (INV) t.y = -t.y;
-      w[q] = t;
-    }
-  } else {
-    V w1 = tw[base];
-    if (INV) w1.y = -w1.y;
-    w[1] = w1;
-    if constexpr (R > 2) w[2] = cmul(w1, w1);
-    if constexpr (R > 3) w[3] = cmul(w[2], w1);
-    if constexpr (R > 4) w[4] = cmul(w[2], w[2]);
-    if constexpr (R > 5) w[5] = cmul(w[4], w1);
-    if constexpr (R > 6) w[6] = cmul(w[4], w[2]);
-    if constexpr (R > 7) w[7] = cmul(w[4], w[3]);
-  }
-}
-
 template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS>
 __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
   constexpr int MAXB = (EPT + R - 1) / R;
@@ -401,12 +374,14 @@ __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
       const int c = b % C;
       const int j = b / C;
       const int k = j % NS;
-      V w[R];
-      if constexpr (NS > 1) ct_twiddles<V, R, INV>(tw, k * TS, w);
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         V x = s[swz(j + q * NR, c, C)];
-        if (NS > 1 && q > 0) x = cmul(x, w[q]);
+        if (NS > 1 && q > 0) {
+          V w = tw[k * q * TS];
+          if (INV) w.y = -w.y;
+          x = cmul(x, w);
+        }
         v[i][q] = x;
       }
       dftr<V, R, INV>(v[i]);
@@ -665,12 +640,14 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
       const int b = tid + i * NTHR;
       if (NB % NTHR == 0 || b < NB) {
         const int c = b % C, j = b / C;
-        V w[RL];
-        ct_twiddles<V, RL, INV>(tw, j, w);
 #pragma unroll
         for (int q = 0; q < RL; ++q) {
           V x = s[swz(j + q * NRL, c, C)];
-          if (q > 0) x = cmul(x, w[q]);
+          if (q > 0) {
+            V w = tw[j * q];
+            if (INV) w.y = -w.y;
+            x = cmul(x, w);
+          }
           v[i][q] = x;
         }
         dftr<V, RL, INV>(v[i]);
@@ -733,12 +710,14 @@ __device__ __forceinline__ bool ct_fft_mapped_mid(V* s, const V* tw, int tid, LD
       const int b = tid + i * NTHR;
       if (NB % NTHR == 0 || b < NB) {
         const int c = b % C, j = b / C;
-        V w[RL];
-        ct_twiddles<V, RL, INV>(tw, j, w);
 #pragma unroll
         for (int q = 0; q < RL; ++q) {
           V x = s[swz(j + q * NRL, c, C)];
-          if (q > 0) x = cmul(x, w[q]);
+          if (q > 0) {
+            V w = tw[j * q];
+            if (INV) w.y = -w.y;
+            x = cmul(x, w);
+          }
           v[i][q] = x;
         }
         dftr<V, RL, INV>(v[i]);

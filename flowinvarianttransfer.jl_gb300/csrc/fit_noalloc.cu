@@ -99,6 +99,20 @@ extern "C" int fit_mode_to_mode_noalloc(int nd, const int64_t* ns, int n_advecte
     fit_set_error("self-advection needs >= nd components (pass adv_hat)");
     return FIT_ERR_ARG;
   }
+  long nm = 1;
+  for (int d = 0; d < nd; ++d) {
+    if (ns[d] < 1) {
+      fit_set_error("grid size must be positive");
+      return FIT_ERR_ARG;
+    }
+    nm *= (long)ns[d];
+    if (nm > FIT_NOALLOC_MAX_MODES) break;
+  }
+  if (nm > FIT_NOALLOC_MAX_MODES) {
+    fit_set_error("fit_mode_to_mode_noalloc: grid has more than %d modes (the fixed scratch limit); "
+                  "use fit_mode_to_mode", FIT_NOALLOC_MAX_MODES);
+    return FIT_ERR_SIZE;
+  }
   // every array is read or written by the kernels: reject NULL tables and host memory up front,
   // before anything is launched
   for (int d = 0; d < nd; ++d) {
@@ -114,20 +128,6 @@ extern "C" int fit_mode_to_mode_noalloc(int nd, const int64_t* ns, int n_advecte
       fit_set_error("%s must be a device pointer (device or managed memory)", names[i]);
       return FIT_ERR_ARG;
     }
-  }
-  long nm = 1;
-  for (int d = 0; d < nd; ++d) {
-    if (ns[d] < 1) {
-      fit_set_error("grid size must be positive");
-      return FIT_ERR_ARG;
-    }
-    nm *= (long)ns[d];
-    if (nm > FIT_NOALLOC_MAX_MODES) break;
-  }
-  if (nm > FIT_NOALLOC_MAX_MODES) {
-    fit_set_error("fit_mode_to_mode_noalloc: grid has more than %d modes (the fixed scratch limit); "
-                  "use fit_mode_to_mode", FIT_NOALLOC_MAX_MODES);
-    return FIT_ERR_SIZE;
   }
   void* scratch = nullptr;
   FIT_TRY(noalloc_scratch_ptr(&scratch));

@@ -464,6 +464,33 @@ int shell_table_i64(const GridDesc& g, const uint16_t* sh, int64_t* out, cudaStr
   return FIT_OK;
 }
 
+// One block per kept row (component, z, y): the row's two x runs [0, K0] and [N0 - K0, N0).
+template <typename E>
+__global__ void __launch_bounds__(128) k_copy_kept_box(const E* __restrict__ src, E* __restrict__ dst, int N0,
+                                                       int N1, int N2, int K0, int K1, int K2) {
+  const int ny = 2 * K1 + 1, nz = 2 * K2 + 1, nx = 2 * K0 + 1;
+  const long r = blockIdx.x;
+  const int iy = (int)(r % ny), iz = (int)((r / ny) % nz), c = (int)(r / ((long)ny * nz));
+  const int y = iy <= K1 ? iy : N1 - ny + iy, z = iz <= K2 ? iz : N2 - nz + iz;
+  const long base = (((long)c * N2 + z) * N1 + y) * (long)N0;
+  for (int ix = threadIdx.x; ix < nx; ix += blockDim.x) {
+    const int x = ix <= K0 ? ix : N0 - nx + ix;
+    dst[base + x] = src[base + x];
+  }
+}
+
+int copy_kept_box(const void* src, void* dst, const int* N, int ncomp, int eb, cudaStream_t st) {
+  const int K0 = N[0] / 3 - 1, K1 = N[1] / 3 - 1, K2 = N[2] / 3 - 1;
+  const long rows = (long)ncomp * (2 * K1 + 1) * (2 * K2 + 1);
+  if (rows <= 0 || K0 < 0) return FIT_OK;
+  if (eb == 16)
+    k_copy_kept_box<uint4><<<(unsigned)rows, 128, 0, st>>>((const uint4*)src, (uint4*)dst, N[0], N[1], N[2], K0, K1, K2);
+  else
+    k_copy_kept_box<uint2><<<(unsigned)rows, 128, 0, st>>>((const uint2*)src, (uint2*)dst, N[0], N[1], N[2], K0, K1, K2);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 __global__ void k_sh_from_i64(const int64_t* __restrict__ idx, long n, int nsh, uint16_t* __restrict__ out,
                               unsigned long long* bad, unsigned* changed) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;

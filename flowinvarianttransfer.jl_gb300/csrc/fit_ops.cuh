@@ -139,6 +139,12 @@ int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_
                 const typename Vec2<T>::t* ceff, int nc, const uint16_t* seff, int nsh, double* partial,
                 long partial_cap, double* out, cudaStream_t st);
 
+// Copies the box of modes every axis keeps under the 2/3 rule (indices [0, K_d] and [N_d - K_d, N_d),
+// K_d = N_d/3 - 1) of ncomp column-major 3D fields from src to the same positions of dst; elements of
+// eb = 8 or 16 bytes. src may be host memory the device can address (pinned, mapped): the device
+// then reads it over the host link itself, one block per kept row.
+int copy_kept_box(const void* src, void* dst, const int* N, int ncomp, int eb, cudaStream_t st);
+
 // Half spectrum on the transform grid -> full N-grid array (user layout), 2/3 mask applied.
 template <typename T>
 int scatter_full(const GridDesc& g, const typename Vec2<T>::t* half, int nf, int two_thirds, void* out,
