@@ -1,4 +1,9 @@
 // Fused shell-to-shell kernels instantiated for cube sizes 64 128 256 512.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
 #include "fit_fused_impl.cuh"
 
 namespace fit {
@@ -52,3 +57,104 @@ int fz_terms_a(int N, const FzArgs& a, const float2* H, const float* kd, const f
 }
 
 }  // namespace fit
+
+// ---- benchmark hook: the x pass alone on synthetic device data ------------------------------------
+namespace {
+
+__global__ void k_bench_fill(float* p, long n, unsigned seed) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    unsigned h = (unsigned)i * 2654435761u ^ seed;
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    p[i] = (float)(h & 0xffffff) / 16777216.0f - 0.5f;
+  }
+}
+
+template <int N>
+int bench_x_pass(long lines, int reps, double* ms, double* bytes) {
+  using namespace fit;
+  const int K = N / 3 - 1, KX = K + 1;
+  FzArgs a;
+  memset(&a, 0, sizeof(a));
+  a.K = K;
+  a.KX = KX;
+  a.KY = 2 * K + 1;
+  a.P1 = (long)KX * a.KY;
+  a.L = lines;
+  a.nsh = 1;
+  a.nb = 1;
+  a.med[0] = 1;
+  a.ext[0][0] = a.ext[0][1] = a.ext[0][2] = (short)K;
+  a.so = 1.0f / ((float)N * N * N);
+  const long Mtot = (long)N * N * N;
+  const size_t gn = (size_t)9 * lines * KX, un = (size_t)(2 * Mtot + lines * (long)N), on = (size_t)3 * lines * KX;
+  float2 *G = nullptr, *out = nullptr, *tw = nullptr;
+  float* U = nullptr;
+  int* err = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = FIT_OK;
+  std::vector<float2> h(N);
+  for (int t = 0; t < N; ++t) {
+    const long double ang = -2.0L * 3.14159265358979323846264338327950288L * t / N;
+    h[t] = make_float2((float)cosl(ang), (float)sinl(ang));
+  }
+  auto ck = [&](cudaError_t e) {
+    if (e != cudaSuccess && rc == FIT_OK) {
+      fit_set_error("x-pass benchmark: %s", cudaGetErrorString(e));
+      rc = FIT_ERR_CUDA;
+    }
+    return rc == FIT_OK;
+  };
+  if (ck(cudaMalloc(&G, gn * 8)) && ck(cudaMalloc(&U, un * 4)) && ck(cudaMalloc(&out, on * 8)) &&
+      ck(cudaMalloc(&tw, (size_t)N * 8)) && ck(cudaMalloc(&err, sizeof(int))) && ck(cudaStreamCreate(&st)) &&
+      ck(cudaEventCreate(&e0)) && ck(cudaEventCreate(&e1)) && ck(cudaMemsetAsync(err, 0, sizeof(int), st)) &&
+      ck(cudaMemcpyAsync(tw, h.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st))) {
+    k_bench_fill<<<1216, 256, 0, st>>>((float*)G, (long)gn * 2, 1u);
+    k_bench_fill<<<1216, 256, 0, st>>>(U, (long)un, 2u);
+    rc = fz_xpass<N>(a, G, U, out, tw, err, st);   // warm-up (kernel attributes)
+    if (rc == FIT_OK && ck(cudaEventRecord(e0, st))) {
+      for (int r = 0; r < reps && rc == FIT_OK; ++r) rc = fz_xpass<N>(a, G, U, out, tw, err, st);
+      float t = 0.f;
+      if (rc == FIT_OK && ck(cudaEventRecord(e1, st)) && ck(cudaStreamSynchronize(st)) &&
+          ck(cudaEventElapsedTime(&t, e0, e1))) {
+        *ms = (double)t / reps;
+        *bytes = 8.0 * 12.0 * (double)lines * KX + 4.0 * 3.0 * (double)N * lines;
+        int hf = 0;
+        if (ck(cudaMemcpy(&hf, err, sizeof(int), cudaMemcpyDeviceToHost)) && hf) {
+          fit_set_error("x-pass benchmark: a bounded wait timed out");
+          rc = FIT_ERR_STATE;
+        }
+      }
+    }
+  }
+  if (st) cudaStreamSynchronize(st);
+  cudaFree(G);
+  cudaFree(U);
+  cudaFree(out);
+  cudaFree(tw);
+  cudaFree(err);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int fit_bench_x_pass(int N, long long lines, int reps, double* ms_per_launch, double* alg_bytes) {
+  if (!ms_per_launch || !alg_bytes || reps < 1 || lines < 16 || lines % 16 != 0 || lines > (long long)N * N) {
+    fit_set_error("x-pass benchmark: need reps >= 1 and 16 <= lines <= N^2, a multiple of 16");
+    return FIT_ERR_ARG;
+  }
+  switch (N) {
+    case 64: return bench_x_pass<64>(lines, reps, ms_per_launch, alg_bytes);
+    case 128: return bench_x_pass<128>(lines, reps, ms_per_launch, alg_bytes);
+    case 256: return bench_x_pass<256>(lines, reps, ms_per_launch, alg_bytes);
+    case 512: return bench_x_pass<512>(lines, reps, ms_per_launch, alg_bytes);
+    default:
+      fit_set_error("x-pass benchmark: transform length %d is not one of 64, 128, 256, 512", N);
+      return FIT_ERR_ARG;
+  }
+}

@@ -561,6 +561,217 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
   }
 }
 
+// ---- xmix, one independent thread group per complex column ---------------------------------------
+// Same arithmetic as k_fz_xmix_reg for transform lengths whose schedule is three radix-8 stages
+// (N = 512), with no block-wide barrier inside the pipeline: each complex column (a pair of lines)
+// belongs to a group of N/8 threads (two warps at N = 512; one radix-8 butterfly per thread and
+// stage) that syncs on its own named barrier and streams its own 2 gradient lines (double buffered)
+// by bulk copies on its own mbarriers; the advecting velocity is read from global memory (L2) into
+// registers ahead of the last inverse stage. The 8 groups of a block share only the twiddle tables,
+// so a group never waits for another group's progress.
+// Layouts chosen so that no shared-memory access has a bank conflict and every address is a
+// per-thread base plus a compile-time offset: each column's 512 elements at e + (e >> 4) (one pad
+// element per 16), which serves the stages' three access shapes (32 consecutive rows; rows 8j + q;
+// four runs of 8 rows 64 apart); twiddles of the middle stage as T1[q][k] = w^(8kq) and of the last
+// stage as T2[q][j] = w^(jq), a warp's lanes reading consecutive entries. The twiddle values are the
+// same table entries as k_fz_xmix_reg's.
+template <int N>
+struct XGTile {
+  static constexpr int C = 8;          // columns (line pairs) per block
+  static constexpr int G = N / 8;      // threads per column group
+  static constexpr int NTHR = C * G;
+  static constexpr bool OK = N == 512 && ct_nst(N) == 3 && ct_radix(N, 0) == 8 && ct_radix(N, 1) == 8 &&
+                             ct_radix(N, 2) == 8;
+  static constexpr int CP = N + N / 16;                              // padded column length
+  static constexpr size_t OFF_T1 = (size_t)C * CP * 8;
+  static constexpr size_t OFF_T2 = OFF_T1 + 7 * 8 * 8;
+  static constexpr size_t OFF_BAR = OFF_T2 + 7 * (size_t)G * 8;      // 2 mbarriers per group
+  static constexpr size_t OFF_G = (OFF_BAR + 2 * C * 8 + 127) / 128 * 128;   // then 2 x C x (2 KX) complex
+};
+
+FIT_D void xg_bar(int id, int nthr) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthr) : "memory"); }
+
+template <int N>
+__global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, const float2* __restrict__ G,
+                                                                   const float* __restrict__ U,
+                                                                   float2* __restrict__ out,
+                                                                   const float2* __restrict__ twg, int* err) {
+  typedef XGTile<N> TT;
+  constexpr int GS = TT::G;            // threads per group = butterflies per stage
+  constexpr int NR = N / 8;            // row stride of a radix-8 stage's inputs
+  static_assert(GS == NR && NR == 64, "one radix-8 butterfly per thread and stage, N = 512");
+  extern __shared__ __align__(128) unsigned char fit_smem_raw[];
+  const int tid = threadIdx.x;
+  const int g = tid / GS, jt = tid % GS;
+  float2* s = reinterpret_cast<float2*>(fit_smem_raw) + (size_t)g * TT::CP;      // this group's column
+  float2* T1 = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_T1);
+  float2* T2 = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_T2);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(fit_smem_raw + TT::OFF_BAR) + 2 * g;   // gradient buffers 0, 1
+  const int KX = a.KX;
+  float2* gbuf = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_G) + (size_t)g * 2 * (2 * KX);
+  const uint32_t gbytes = (uint32_t)(2 * KX) * 8u;
+  const int b = blockIdx.x;
+  const int ex = a.ext[b][0];
+  const long Mtot = (long)N * N * N;
+  const long la = (long)blockIdx.z * 2 * TT::C + 2 * g;   // this group's lines la, la + 1
+  U += (long)a.uidx[b] * 3 * Mtot;
+  const bool lead = jt == 0;
+  const int gid = 1 + g;                                    // named barrier of the group
+  for (int t = tid; t < 7 * 8; t += TT::NTHR) T1[t] = twg[(t % 8) * (t / 8 + 1) * (N / 64)];
+  for (int t = tid; t < 7 * GS; t += TT::NTHR) T2[t] = twg[(t % GS) * (t / GS + 1)];
+  if (lead) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();   // the only block-wide barrier: twiddle tables and mbarriers ready
+  if (lead) {
+    mbar_expect_tx(&bar[0], gbytes);
+    bulk_g2s(gbuf, G + (((long)b * 9) * a.L + la) * KX, gbytes, &bar[0]);
+  }
+  // per-thread bases of the three padded access shapes: rows jt + 64q (P = jt + (jt >> 4) + 68q),
+  // rows 8 jt + q (P = 8 jt + (jt >> 1) + q), rows 64 (jt >> 3) + (jt & 7) + 8q
+  // (P = 68 (jt >> 3) + (jt & 7) + 8q + (q >> 1))
+  const int pA = jt + (jt >> 4), pB = 8 * jt + (jt >> 1), pC = 68 * (jt >> 3) + (jt & 7);
+  const int k1 = jt & 7;
+  // waits as in k_fz_xmix_reg: a first wait that runs out flags the launch and is followed by a
+  // full-bound wait; a thread whose second wait runs out is broken (the lead then issues nothing
+  // more) and the group carries on with whatever the buffers hold, all indices data-independent
+  bool failed = false, broken = false;
+  int issued0 = 1, issued1 = 0;
+  float2 acc[8];
+  float2 v[8];
+  for (int t = 0; t < 9; ++t) {
+    const int c = t / 3, j = t % 3, buf = t & 1;
+    if (j == 0) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = make_float2(0.f, 0.f);
+    }
+    if (lead && t + 1 < 9 && !broken) {   // next gradient lines into the other buffer (read at step t - 1)
+      const int c1 = (t + 1) / 3, j1 = (t + 1) % 3, nb1 = (t + 1) & 1;
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[nb1], gbytes);
+      bulk_g2s(gbuf + nb1 * (2 * KX), G + ((((long)b * 3 + c1) * 3 + j1) * a.L + la) * KX, gbytes, &bar[nb1]);
+      if (nb1) ++issued1;
+      else ++issued0;
+    }
+    if (!mbar_wait_or_flag(&bar[buf], (uint32_t)((t >> 1) & 1), a.wlim, failed)) broken = true;
+    // stage 0 of the inverse transform: inputs k = jt + 64q of the Hermitian pair z = A + iB
+    const float2* ga = gbuf + buf * (2 * KX);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = jt + NR * q;
+      const bool cj = 2 * k > N;
+      const int kk = cj ? N - k : k;
+      float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+      if (kk <= ex) {
+        A = ga[kk];
+        B = ga[KX + kk];
+        if (cj) { A.y = -A.y; B.y = -B.y; }
+        if (k == 0) { A.y = 0.f; B.y = 0.f; }
+      }
+      v[q] = make_float2(A.x - B.y, A.y + B.x);
+    }
+    dftr<float2, 8, true>(v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s[pB + q] = v[q];
+    xg_bar(gid, GS);
+    // stage 1 (span 8)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float2 x = s[pA + 68 * q];
+      if (q > 0 && k1 > 0) {
+        float2 w = T1[8 * (q - 1) + k1];
+        w.y = -w.y;
+        x = cmul(x, w);
+      }
+      v[q] = x;
+    }
+    dftr<float2, 8, true>(v);
+    // the velocity at this thread's outputs x = jt + 64q of both lines, read ahead of the last stage
+    float ua[8], ub[8];
+    {
+      const float* Ua = U + (long)j * Mtot + la * N + jt;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        ua[q] = __ldg(Ua + NR * q);
+        ub[q] = __ldg(Ua + N + NR * q);
+      }
+    }
+    xg_bar(gid, GS);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s[pC + 8 * q + (q >> 1)] = v[q];
+    xg_bar(gid, GS);
+    // stage 2 (span 64): outputs x = jt + 64q, accumulated against the velocity
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float2 x = s[pA + 68 * q];
+      if (q > 0) {
+        float2 w = T2[GS * (q - 1) + jt];
+        w.y = -w.y;
+        x = cmul(x, w);
+      }
+      v[q] = x;
+    }
+    dftr<float2, 8, true>(v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      acc[q].x += ua[q] * v[q].x;
+      acc[q].y += ub[q] * v[q].y;
+    }
+    xg_bar(gid, GS);   // the column is free for the next stage-0 writes
+    if (j == 2) {   // forward transform of the product, kx <= K of both lines
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = acc[q];
+      dftr<float2, 8, false>(v);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s[pB + q] = v[q];
+      xg_bar(gid, GS);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float2 x = s[pA + 68 * q];
+        if (q > 0 && k1 > 0) x = cmul(x, T1[8 * (q - 1) + k1]);
+        v[q] = x;
+      }
+      dftr<float2, 8, false>(v);
+      xg_bar(gid, GS);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s[pC + 8 * q + (q >> 1)] = v[q];
+      xg_bar(gid, GS);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float2 x = s[pA + 68 * q];
+        if (q > 0) x = cmul(x, T2[GS * (q - 1) + jt]);
+        v[q] = x;
+      }
+      dftr<float2, 8, false>(v);
+      xg_bar(gid, GS);   // every stage-2 read of the column is done before it is overwritten
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s[pA + 68 * q] = v[q];   // Z(k), k = jt + 64q
+      xg_bar(gid, GS);
+      const long obase = ((long)b * 3 + c) * a.L;
+      const float hs = 0.5f * a.so;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = jt + NR * q;
+        if (k < KX) {
+          const int e = k == 0 ? 0 : N - k;
+          const float2 zk = v[q];
+          const float2 zn = s[e + (e >> 4)];
+          out[(obase + la) * KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+          out[(obase + la + 1) * KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+        }
+      }
+      xg_bar(gid, GS);   // the column is free for the next transform
+    }
+  }
+  if (failed) atomicExch(err, 1);
+  if (lead) {   // no copy may still be landing when the block exits: the last issued phase of each
+    mbar_wait_bounded(&bar[0], (uint32_t)((issued0 - 1) & 1), FIT_WAIT_CYCLES / 10);
+    if (issued1 > 0) mbar_wait_bounded(&bar[1], (uint32_t)((issued1 - 1) & 1), FIT_WAIT_CYCLES / 10);
+  }
+}
+
 // ---- yfwd --------------------------------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(FzArgs a, const float2* __restrict__ in,
@@ -924,6 +1135,17 @@ int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, cons
   bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
   FzArgs aw = a;
   aw.wlim = fit_wait_cycles();
+  typedef XGTile<N> XG;
+  const char* envr = getenv("FIT_XMIX_REG");   // selects the block-synchronous register form
+  if constexpr (XG::OK) {
+    const size_t smg = XG::OFF_G + 2 * (size_t)XG::C * (2 * a.KX) * 8;
+    if (reg && !(envr && envr[0] == '1') && smg <= 227 * 1024 && (a.L % (2 * XG::C)) == 0) {
+      FIT_TRY(ct_prep_fused(k_fz_xmix_grp<N>, smg, XG::NTHR));
+      k_fz_xmix_grp<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XG::C))), XG::NTHR, smg, st>>>(aw, G, U, out, tw, err);
+      FIT_LAUNCH_CHECK();
+      return FIT_OK;
+    }
+  }
   if constexpr (XR::OK) {
     if (reg) {
       FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
