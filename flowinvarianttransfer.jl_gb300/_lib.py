@@ -19,7 +19,7 @@ EXPORTS = [
     "fit_batch_create", "fit_batch_destroy", "fit_batch_add_flux", "fit_batch_run", "fit_batch_run_eager", "fit_batch_info",
     "fit_autotune_enable", "fit_autotune_clear", "fit_autotune_info", "fit_autotune_entry",
     "fit_partial_fluxes_batched", "fit_band_to_band", "fit_stress_residual",
-    "fit_set_shell_index", "fit_shell_to_shell_indexed", "fit_bench_x_pass",
+    "fit_set_shell_index", "fit_shell_to_shell_indexed", "fit_bench_fused_pass",
 ]
 
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -82,7 +82,7 @@ def _declare(lib):
     lib.fit_autotune_clear.argtypes = []
     lib.fit_autotune_info.argtypes = [C.POINTER(i64), C.POINTER(i64), dp, dp]
     lib.fit_autotune_entry.argtypes = [i64, C.POINTER(i64), dp]
-    lib.fit_bench_x_pass.argtypes = [i32, C.c_longlong, i32, dp, dp]
+    lib.fit_bench_fused_pass.argtypes = [i32, i32, C.c_longlong, i32, dp, dp]
     lib.fit_band_to_band.argtypes = [vp, vp, vp, dp, i32, C.c_double, u32, i32, i32, vp, vp, vp, i32]
     lib.fit_partial_fluxes_batched.argtypes = [vp, vp, i32, C.POINTER(i32), i32, dp, i32, u32, i32, vp, i32]
     lib.fit_mlp_adam.argtypes = [vp, vp, vp, vp, i32, f32, f32, f32, f32, vp]

@@ -72,24 +72,29 @@ __global__ void k_bench_fill(float* p, long n, unsigned seed) {
 }
 
 template <int N>
-int bench_x_pass(long lines, int reps, double* ms, double* bytes) {
+int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   using namespace fit;
-  const int K = N / 3 - 1, KX = K + 1;
+  const int K = N / 3 - 1, KX = K + 1, KY = 2 * K + 1;
+  const long P1 = (long)KX * KY, L = (long)N * N;
   FzArgs a;
   memset(&a, 0, sizeof(a));
   a.K = K;
   a.KX = KX;
-  a.KY = 2 * K + 1;
-  a.P1 = (long)KX * a.KY;
-  a.L = lines;
+  a.KY = KY;
+  a.P1 = P1;
+  a.L = pass == 0 ? units : L;
   a.nsh = 1;
   a.nb = 1;
   a.med[0] = 1;
   a.ext[0][0] = a.ext[0][1] = a.ext[0][2] = (short)K;
   a.so = 1.0f / ((float)N * N * N);
   const long Mtot = (long)N * N * N;
-  const size_t gn = (size_t)9 * lines * KX, un = (size_t)(2 * Mtot + lines * (long)N), on = (size_t)3 * lines * KX;
-  float2 *G = nullptr, *out = nullptr, *tw = nullptr;
+  // pass 0 (x pass): G (9 lines x KX per line), U (3 velocity fields, the last one sliced), out (3 x KX);
+  // pass 1 (y inverse): the six z-pass outputs of all N planes in, nine y-pass outputs out
+  const size_t in_n = pass == 0 ? (size_t)9 * units * KX : (size_t)6 * N * P1;
+  const size_t un = pass == 0 ? (size_t)(2 * Mtot + units * (long)N) : (size_t)KY;
+  const size_t on = pass == 0 ? (size_t)3 * units * KX : (size_t)9 * L * KX;
+  float2 *in = nullptr, *out = nullptr, *tw = nullptr;
   float* U = nullptr;
   int* err = nullptr;
   cudaStream_t st = nullptr;
@@ -102,35 +107,40 @@ int bench_x_pass(long lines, int reps, double* ms, double* bytes) {
   }
   auto ck = [&](cudaError_t e) {
     if (e != cudaSuccess && rc == FIT_OK) {
-      fit_set_error("x-pass benchmark: %s", cudaGetErrorString(e));
+      fit_set_error("fused-pass benchmark: %s", cudaGetErrorString(e));
       rc = FIT_ERR_CUDA;
     }
     return rc == FIT_OK;
   };
-  if (ck(cudaMalloc(&G, gn * 8)) && ck(cudaMalloc(&U, un * 4)) && ck(cudaMalloc(&out, on * 8)) &&
+  auto launch = [&]() -> int {
+    if (pass == 0) return fz_xpass<N>(a, in, U, out, tw, err, st);
+    return fz_yinv<N>(a, in, U, out, tw, err, (int)units, st);
+  };
+  if (ck(cudaMalloc(&in, in_n * 8)) && ck(cudaMalloc(&U, un * 4)) && ck(cudaMalloc(&out, on * 8)) &&
       ck(cudaMalloc(&tw, (size_t)N * 8)) && ck(cudaMalloc(&err, sizeof(int))) && ck(cudaStreamCreate(&st)) &&
       ck(cudaEventCreate(&e0)) && ck(cudaEventCreate(&e1)) && ck(cudaMemsetAsync(err, 0, sizeof(int), st)) &&
       ck(cudaMemcpyAsync(tw, h.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st))) {
-    k_bench_fill<<<1216, 256, 0, st>>>((float*)G, (long)gn * 2, 1u);
+    k_bench_fill<<<1216, 256, 0, st>>>((float*)in, (long)in_n * 2, 1u);
     k_bench_fill<<<1216, 256, 0, st>>>(U, (long)un, 2u);
-    rc = fz_xpass<N>(a, G, U, out, tw, err, st);   // warm-up (kernel attributes)
+    rc = launch();   // warm-up (kernel attributes)
     if (rc == FIT_OK && ck(cudaEventRecord(e0, st))) {
-      for (int r = 0; r < reps && rc == FIT_OK; ++r) rc = fz_xpass<N>(a, G, U, out, tw, err, st);
+      for (int r = 0; r < reps && rc == FIT_OK; ++r) rc = launch();
       float t = 0.f;
       if (rc == FIT_OK && ck(cudaEventRecord(e1, st)) && ck(cudaStreamSynchronize(st)) &&
           ck(cudaEventElapsedTime(&t, e0, e1))) {
         *ms = (double)t / reps;
-        *bytes = 8.0 * 12.0 * (double)lines * KX + 4.0 * 3.0 * (double)N * lines;
+        *bytes = pass == 0 ? 8.0 * 12.0 * (double)units * KX + 4.0 * 3.0 * (double)N * units
+                           : 8.0 * ((double)units * (6.0 * P1 + 9.0 * (double)N * KX));
         int hf = 0;
         if (ck(cudaMemcpy(&hf, err, sizeof(int), cudaMemcpyDeviceToHost)) && hf) {
-          fit_set_error("x-pass benchmark: a bounded wait timed out");
+          fit_set_error("fused-pass benchmark: a bounded wait timed out");
           rc = FIT_ERR_STATE;
         }
       }
     }
   }
   if (st) cudaStreamSynchronize(st);
-  cudaFree(G);
+  cudaFree(in);
   cudaFree(U);
   cudaFree(out);
   cudaFree(tw);
@@ -143,18 +153,22 @@ int bench_x_pass(long lines, int reps, double* ms, double* bytes) {
 
 }  // namespace
 
-extern "C" int fit_bench_x_pass(int N, long long lines, int reps, double* ms_per_launch, double* alg_bytes) {
-  if (!ms_per_launch || !alg_bytes || reps < 1 || lines < 16 || lines % 16 != 0 || lines > (long long)N * N) {
-    fit_set_error("x-pass benchmark: need reps >= 1 and 16 <= lines <= N^2, a multiple of 16");
+extern "C" int fit_bench_fused_pass(int pass, int N, long long units, int reps, double* ms_per_launch,
+                                    double* alg_bytes) {
+  const long long maxu = pass == 0 ? (long long)N * N : (long long)N;
+  if (!ms_per_launch || !alg_bytes || reps < 1 || (pass != 0 && pass != 1) || units < 1 || units > maxu ||
+      (pass == 0 && units % 16 != 0)) {
+    fit_set_error("fused-pass benchmark: pass 0 (x lines: a multiple of 16, at most N^2) or 1 (z planes: at "
+                  "most N), reps >= 1");
     return FIT_ERR_ARG;
   }
   switch (N) {
-    case 64: return bench_x_pass<64>(lines, reps, ms_per_launch, alg_bytes);
-    case 128: return bench_x_pass<128>(lines, reps, ms_per_launch, alg_bytes);
-    case 256: return bench_x_pass<256>(lines, reps, ms_per_launch, alg_bytes);
-    case 512: return bench_x_pass<512>(lines, reps, ms_per_launch, alg_bytes);
+    case 64: return bench_pass<64>(pass, units, reps, ms_per_launch, alg_bytes);
+    case 128: return bench_pass<128>(pass, units, reps, ms_per_launch, alg_bytes);
+    case 256: return bench_pass<256>(pass, units, reps, ms_per_launch, alg_bytes);
+    case 512: return bench_pass<512>(pass, units, reps, ms_per_launch, alg_bytes);
     default:
-      fit_set_error("x-pass benchmark: transform length %d is not one of 64, 128, 256, 512", N);
+      fit_set_error("fused-pass benchmark: transform length %d is not one of 64, 128, 256, 512", N);
       return FIT_ERR_ARG;
   }
 }

@@ -181,6 +181,19 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
       });
 }
 
+// The y-inverse pass of a batch over z planes [0, nz), one block per (mediator, output, plane, kx tile).
+template <int N>
+int fz_yinv(const FzArgs& a, const float2* in, const float* kd, float2* out, const float2* tw, int* err, int nz,
+            cudaStream_t st) {
+  typedef FzTile<N> TT;
+  (void)err;
+  FIT_TRY(ct_prep_fused(k_fz_yinv<N>, TT::SMEM, TT::NTHR));
+  const unsigned nkt = (unsigned)((a.KX + TT::C - 1) / TT::C);
+  k_fz_yinv<N><<<dim3(a.nb, 9, nkt * (unsigned)nz), TT::NTHR, TT::SMEM, st>>>(a, in, kd, out, tw);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 // ---- xmix: inverse x transforms, product with the advecting velocity, forward x transform -----
 template <int N>
 __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const float2* __restrict__ G,
@@ -1189,9 +1202,8 @@ int fz_terms(const FzArgs& a, const float2* H, const float* kd, const float* U, 
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_YINV, cpx * a.nb * (6.0 * N * a.P1 + 9.0 * L * a.KX), st);
-  k_fz_yinv<N><<<dim3(a.nb, 9, nkt * N), TT::NTHR, sm, st>>>(a, bufA, kd, bufB, tw);
+  FIT_TRY(fz_yinv<N>(a, bufA, kd, bufB, tw, err, N, st));
   fit_prof_end(st);
-  FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_XMIX, cpx * a.nb * (9.0 * L * a.KX + 3.0 * L * a.KX) + 4.0 * 3.0 * N * L * 2, st);
   FIT_TRY(fz_xpass<N>(a, bufB, U, bufA, tw, err, st));
   fit_prof_end(st);
@@ -1239,9 +1251,8 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_YINV, yin_b, st);
-  k_fz_yinv<N><<<dim3(a.nb, 9, nkt * N), TT::NTHR, sm, st>>>(a, bufA, kd, bufB, tw);
+  FIT_TRY(fz_yinv<N>(a, bufA, kd, bufB, tw, err, N, st));
   fit_prof_end(st);
-  FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_XMIX,
                  cpx * a.nb * (9.0 * (double)N * N * a.KX + 3.0 * (double)N * N * a.KX) + 4.0 * 3.0 * N * N * N, st);
   FIT_TRY(fz_xpass<N>(a, bufB, U, bufA, tw, err, st));

@@ -223,14 +223,15 @@ int fit_autotune_info(int64_t* n_entries, int64_t* n_runtime_engine, double* ms_
  * bytes, engine (0 compile-time, 1 runtime), C, elements per thread, radix order; ms = best, default. */
 int fit_autotune_entry(int64_t i, int64_t* fields, double* ms);
 
-/* Benchmark hook (no counterpart in the reference): times the x pass of the fused shell-to-shell
- * pipeline alone (inverse x transforms, product with the advecting velocity, forward x transform)
- * on synthetic device data: one mediator of full x extent over `lines` lines (a multiple of 16, at
- * most N^2) of an N^3 grid under the 2/3 rule, N in {64, 128, 256, 512}; reps launches after one
- * warm-up. ms_per_launch = mean launch time, alg_bytes = the launch's algorithmic bytes (nine
- * gradient lines read and three output lines written per line, the velocity read once). Allocates
- * its buffers for the call (about 2.3 GB at N = 512, lines = 65536) and frees them. */
-int fit_bench_x_pass(int N, long long lines, int reps, double* ms_per_launch, double* alg_bytes);
+/* Benchmark hook (no counterpart in the reference): times one kernel of the fused shell-to-shell
+ * pipeline alone on synthetic device data, one mediator of full extent on an N^3 grid under the
+ * 2/3 rule, N in {64, 128, 256, 512}; reps launches after one warm-up. pass 0: the x pass (inverse
+ * x transforms, product with the advecting velocity, forward x transform) over `units` x lines (a
+ * multiple of 16, at most N^2); pass 1: the y-inverse pass over `units` z planes (at most N).
+ * ms_per_launch = mean launch time, alg_bytes = the launch's algorithmic bytes. Allocates its
+ * buffers for the call and frees them (about 2.3 GB for the x pass at N = 512 over 65536 lines,
+ * 4.6 GB for the y pass at N = 512). */
+int fit_bench_fused_pass(int pass, int N, long long units, int reps, double* ms_per_launch, double* alg_bytes);
 
 /* ---- learned subfilter-stress closure (no counterpart in the reference) -------------------------
  * A pointwise MLP 9 -> 64 -> 64 -> 6 (ReLU) maps the filtered velocity-gradient tensor A_ij = d_j ū_i
