@@ -258,9 +258,17 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ P
 // them to an mbarrier, every thread waits on it (clock-bounded) and reads its accumulator row from
 // tensor memory. Layer widths: 16 (9 features) -> 64 -> 64 -> 16 (6 outputs). The 64 tensor-memory
 // columns are reused by all three layers (each accumulator is read out before the next MMA).
+// The biases ride in the MMAs: columns 9 and 10 of the layer-1 A tile hold ones, and each bias b is
+// split into BF16 parts hi = bf16(b), lo = bf16(b - hi) placed in those columns of a weight tile
+// (W1 itself for layer 1; one K = 16 step of A1 against the bias tiles B2b / B3b for layers 2 and 3,
+// whose other columns are zero), so the accumulator leaves the tensor cores as W x + b with b exact
+// to about 2^-17 of |b|. The epilogue then only rounds to BF16 pairs and applies the ReLU on the
+// packed pairs (relu and rounding commute), about half the instructions per point of an epilogue
+// that adds the bias and clamps in FP32.
 struct MlpTcSmem {
   __nv_bfloat16 W1[64 * 16], W2[64 * 64], W3[16 * 64], A1[128 * 16], A2[128 * 64];   // canonical layouts
-  float b1[64], b2[64], b3[8], sc[9], osc[6];
+  __nv_bfloat16 B2b[64 * 16], B3b[16 * 16];   // bias tiles of layers 2 and 3 (columns 9, 10)
+  float sc[9], osc[6];
   uint64_t bar;
   uint32_t tmem;
 };
@@ -274,16 +282,30 @@ FIT_D void st_bf16_at(__nv_bfloat16* tile, uint32_t off, float v) {
   *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(tile) + off) = __float2bfloat16_rn(v);
 }
 
-// relu(D + b) of this thread's 64-column accumulator row -> its row of the next layer's A tile.
-FIT_D void hidden_to_a(uint32_t tl, const float* b, __nv_bfloat16* A2, int row) {
+// The BF16 parts of a bias value: hi = bf16(b), lo = bf16(b - hi).
+FIT_D void bias_split(float b, float* hi, float* lo) {
+  const float h = __bfloat162float(__float2bfloat16_rn(b));
+  *hi = h;
+  *lo = b - h;
+}
+
+// relu(D) of this thread's 64-column accumulator row (bias included) -> its row of the next layer's
+// A tile: BF16 pairs, clamped as pairs.
+FIT_D void hidden_to_a(uint32_t tl, __nv_bfloat16* A2, int row) {
+  const __nv_bfloat162 zero = __floats2bfloat162_rn(0.f, 0.f);
 #pragma unroll
   for (int c4 = 0; c4 < 4; ++c4) {
     float d[16];
     tmem_ld16(tl + 16 * c4, d);
+    uint32_t w[8];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) d[i] = fmaxf(d[i] + b[16 * c4 + i], 0.f);
-    st_chunk(A2, umma_off(row, 16 * c4, 64), d);
-    st_chunk(A2, umma_off(row, 16 * c4 + 8, 64), d + 8);
+    for (int i = 0; i < 8; ++i) {
+      __nv_bfloat162 v = __hmax2(__floats2bfloat162_rn(d[2 * i], d[2 * i + 1]), zero);
+      w[i] = *reinterpret_cast<uint32_t*>(&v);
+    }
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(A2) + umma_off(row, 16 * c4, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(A2) + umma_off(row, 16 * c4 + 8, 64)) =
+        make_uint4(w[4], w[5], w[6], w[7]);
   }
 }
 
@@ -295,15 +317,29 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
   extern __shared__ __align__(128) unsigned char mlp_tc_raw[];
   MlpTcSmem& S = *reinterpret_cast<MlpTcSmem*>(mlp_tc_raw);
   const int tid = threadIdx.x, warp = tid >> 5;
-  for (int i = tid; i < 64 * 16; i += 128) st_bf16_at(S.W1, umma_off(i / 16, i % 16, 16), Pm[MlpOff::W1 + i]);
+  for (int i = tid; i < 64 * 16; i += 128) {   // W1 with b1 in columns 9 (hi) and 10 (lo)
+    const int r = i / 16, c = i % 16;
+    float w = Pm[MlpOff::W1 + i];
+    if (c == 9 || c == 10) {
+      float hi, lo;
+      bias_split(Pm[MlpOff::B1 + r], &hi, &lo);
+      w = c == 9 ? hi : lo;
+    }
+    st_bf16_at(S.W1, umma_off(r, c, 16), w);
+  }
   for (int i = tid; i < 64 * 64; i += 128) st_bf16_at(S.W2, umma_off(i / 64, i % 64, 64), Pm[MlpOff::W2 + i]);
   for (int i = tid; i < 16 * 64; i += 128)   // outputs padded 8 -> 16 rows (rows 6.. never read out)
     st_bf16_at(S.W3, umma_off(i / 64, i % 64, 64), i < 8 * 64 ? Pm[MlpOff::W3 + i] : 0.f);
-  if (tid < 64) {
-    S.b1[tid] = Pm[MlpOff::B1 + tid];
-    S.b2[tid] = Pm[MlpOff::B2 + tid];
+  for (int i = tid; i < 64 * 16; i += 128) {   // bias tiles: b2, b3 split into columns 9 and 10
+    const int r = i / 16, c = i % 16;
+    float hi, lo;
+    bias_split(Pm[MlpOff::B2 + r], &hi, &lo);
+    st_bf16_at(S.B2b, umma_off(r, c, 16), c == 9 ? hi : (c == 10 ? lo : 0.f));
+    if (r < 16) {
+      bias_split(r < 8 ? Pm[MlpOff::B3 + r] : 0.f, &hi, &lo);
+      st_bf16_at(S.B3b, umma_off(r, c, 16), c == 9 ? hi : (c == 10 ? lo : 0.f));
+    }
   }
-  if (tid < 8) S.b3[tid] = Pm[MlpOff::B3 + tid];
   if (tid < 9) S.sc[tid] = in_scale[tid];
   if (tid < 6) S.osc[tid] = 1.f / t_scale[tid];
   if (tid == 0) {
@@ -322,6 +358,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
   const uint32_t tl = tbase + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
   const uint32_t aA1 = smem_u32(S.A1), aA2 = smem_u32(S.A2);
   const uint32_t aW1 = smem_u32(S.W1), aW2 = smem_u32(S.W2), aW3 = smem_u32(S.W3);
+  const uint32_t aB2 = smem_u32(S.B2b), aB3 = smem_u32(S.B3b);
   constexpr uint32_t ID64 = umma_idesc_bf16(128, 64), ID16 = umma_idesc_bf16(128, 16);
   uint32_t phase = 0;
   bool failed = false;
@@ -363,8 +400,10 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
     if (homog) {   // the network sees the direction of the scaled gradient tensor
       const float inv = q > 0.f ? 1.f / sqrtf(q) : 0.f;
 #pragma unroll
-      for (int f = 0; f < 16; ++f) v[f] *= inv;
+      for (int f = 0; f < 9; ++f) v[f] *= inv;
     }
+    v[9] = 1.f;    // the bias columns
+    v[10] = 1.f;
     st_chunk(S.A1, umma_off(tid, 0, 16), v);
     st_chunk(S.A1, umma_off(tid, 8, 16), v + 8);
     publish_a();
@@ -374,23 +413,25 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
       umma_commit(&S.bar);
     }
     wait_mma();
-    hidden_to_a(tl, S.b1, S.A2, tid);
+    hidden_to_a(tl, S.A2, tid);
     publish_a();
     if (tid == 0) {
       tc_fence_after();
+      umma_bf16(tbase, umma_desc(aA1, 128, 256), umma_desc(aB2, 128, 256), ID64, false);   // b2 (ones x bias)
 #pragma unroll
       for (int s = 0; s < 4; ++s)
-        umma_bf16(tbase, umma_desc(aA2 + 256 * s, 128, 1024), umma_desc(aW2 + 256 * s, 128, 1024), ID64, s > 0);
+        umma_bf16(tbase, umma_desc(aA2 + 256 * s, 128, 1024), umma_desc(aW2 + 256 * s, 128, 1024), ID64, true);
       umma_commit(&S.bar);
     }
     wait_mma();
-    hidden_to_a(tl, S.b2, S.A2, tid);   // layer 2 has read A2: its MMAs completed
+    hidden_to_a(tl, S.A2, tid);   // layer 2 has read A2: its MMAs completed
     publish_a();
     if (tid == 0) {
       tc_fence_after();
+      umma_bf16(tbase, umma_desc(aA1, 128, 256), umma_desc(aB3, 128, 256), ID16, false);   // b3
 #pragma unroll
       for (int s = 0; s < 4; ++s)
-        umma_bf16(tbase, umma_desc(aA2 + 256 * s, 128, 1024), umma_desc(aW3 + 256 * s, 128, 1024), ID16, s > 0);
+        umma_bf16(tbase, umma_desc(aA2 + 256 * s, 128, 1024), umma_desc(aW3 + 256 * s, 128, 1024), ID16, true);
       umma_commit(&S.bar);
     }
     wait_mma();
@@ -400,7 +441,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(const float* __restrict_
       float part = 0.f;
 #pragma unroll
       for (int o = 0; o < 6; ++o) {
-        float tau = (y[o] + S.b3[o]) * sn * S.osc[o];
+        float tau = y[o] * sn * S.osc[o];
         if (clark != 0.f) tau += clark * gradient_model_stress_r(o, A);
         if (Y) Y[(long)o * ld + p] = tau;
         part += stress_dot_strain_r(o, tau, A);
