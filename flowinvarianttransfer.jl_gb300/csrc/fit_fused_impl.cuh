@@ -26,6 +26,7 @@
 #include <stdlib.h>
 
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 #include "fit_fft.cuh"
@@ -582,12 +583,16 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
 // by bulk copies on its own mbarriers; the advecting velocity is read from global memory (L2) into
 // registers ahead of the last inverse stage. The 8 groups of a block share only the twiddle tables,
 // so a group never waits for another group's progress.
-// Layouts chosen so that no shared-memory access has a bank conflict and every address is a
-// per-thread base plus a compile-time offset: each column's 512 elements at e + (e >> 4) (one pad
-// element per 16), which serves the stages' three access shapes (32 consecutive rows; rows 8j + q;
-// four runs of 8 rows 64 apart); twiddles of the middle stage as T1[q][k] = w^(8kq) and of the last
-// stage as T2[q][j] = w^(jq), a warp's lanes reading consecutive entries. The twiddle values are the
-// same table entries as k_fz_xmix_reg's.
+// Column layout: row e = 64 e2 + 8 e1 + e0 of a 512-element column sits at
+//   P(e) = 16 (e >> 4) + ((e0 ^ g) | (h << 3)),  g = (e1 >> 1) | ((e2 & 1) << 2),  h = (e1 ^ e2) & 1,
+// a bijection inside each 16-row block. A half-warp's 16 eight-byte accesses then fall in 16
+// different bank pairs in each of the stages' three access shapes: A, rows jt + 64q (32 consecutive
+// rows per warp); B, rows 8 jt + q; C, rows 64 (jt >> 3) + (jt & 7) + 8q. No padding layout serves
+// all three (one pad per 16 rows leaves C two-way conflicted). Each access is a per-thread base
+// and a compile-time q: A at 64q + base(q & 1), B at base ^ q, C at (base ^ c(q)) + 16 (q >> 1).
+// Twiddles of the middle stage as T1[q][k] = w^(8kq) and of the last stage as T2[q][j] = w^(jq), a
+// warp's lanes reading consecutive entries; the values are the same table entries as
+// k_fz_xmix_reg's.
 template <int N>
 struct XGTile {
   static constexpr int C = 8;          // columns (line pairs) per block
@@ -595,7 +600,7 @@ struct XGTile {
   static constexpr int NTHR = C * G;
   static constexpr bool OK = N == 512 && ct_nst(N) == 3 && ct_radix(N, 0) == 8 && ct_radix(N, 1) == 8 &&
                              ct_radix(N, 2) == 8;
-  static constexpr int CP = N + N / 16;                              // padded column length
+  static constexpr int CP = N;                                       // column length (XOR layout)
   static constexpr size_t OFF_T1 = (size_t)C * CP * 8;
   static constexpr size_t OFF_T2 = OFF_T1 + 7 * 8 * 8;
   static constexpr size_t OFF_BAR = OFF_T2 + 7 * (size_t)G * 8;      // 2 mbarriers per group
@@ -603,6 +608,42 @@ struct XGTile {
 };
 
 FIT_D void xg_bar(int id, int nthr) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthr) : "memory"); }
+
+// P(e) of k_fz_xmix_grp's column layout
+FIT_D int xg_swz(int e) {
+  return (e & ~15) | (((e & 7) ^ (((e >> 4) & 3) | (((e >> 6) & 1) << 2))) | ((((e >> 3) ^ (e >> 6)) & 1) << 3));
+}
+
+// f(std::integral_constant<int, q>) for q = 0 .. Q-1, in order
+template <int Q, class F>
+FIT_D void xg_for(F&& f) {
+  if constexpr (Q > 0) {
+    xg_for<Q - 1>(f);
+    f(std::integral_constant<int, Q - 1>{});
+  }
+}
+
+// The float2 at shared byte address (base ^ X) + OFF. The XOR happens inside the access, so a
+// shape keeps one base register instead of the compiler hoisting its eight XOR'd addresses out of
+// the transform loop. Loads are ordered against the group barriers and the stores (all volatile).
+template <int X, int OFF>
+FIT_D float2 xg_ld(uint32_t base) {
+  float2 v;
+  if constexpr (X == 0)
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(base), "n"(OFF));
+  else
+    asm volatile("{\n\t.reg .b32 xa;\n\txor.b32 xa, %2, %3;\n\tld.shared.v2.f32 {%0, %1}, [xa+%4];\n\t}"
+                 : "=f"(v.x), "=f"(v.y) : "r"(base), "n"(X), "n"(OFF));
+  return v;
+}
+template <int X, int OFF>
+FIT_D void xg_st(uint32_t base, float2 v) {
+  if constexpr (X == 0)
+    asm volatile("st.shared.v2.f32 [%0+%1], {%2, %3};" ::"r"(base), "n"(OFF), "f"(v.x), "f"(v.y) : "memory");
+  else
+    asm volatile("{\n\t.reg .b32 xa;\n\txor.b32 xa, %0, %1;\n\tst.shared.v2.f32 [xa+%2], {%3, %4};\n\t}"
+                 ::"r"(base), "n"(X), "n"(OFF), "f"(v.x), "f"(v.y) : "memory");
+}
 
 template <int N>
 __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, const float2* __restrict__ G,
@@ -642,11 +683,21 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
     mbar_expect_tx(&bar[0], gbytes);
     bulk_g2s(gbuf, G + (((long)b * 9) * a.L + la) * KX, gbytes, &bar[0]);
   }
-  // per-thread bases of the three padded access shapes: rows jt + 64q (P = jt + (jt >> 4) + 68q),
-  // rows 8 jt + q (P = 8 jt + (jt >> 1) + q), rows 64 (jt >> 3) + (jt & 7) + 8q
-  // (P = 68 (jt >> 3) + (jt & 7) + 8q + (q >> 1))
-  const int pA = jt + (jt >> 4), pB = 8 * jt + (jt >> 1), pC = 68 * (jt >> 3) + (jt & 7);
-  const int k1 = jt & 7;
+  // per-thread bases of the three access shapes (l = jt & 7, u = jt >> 3): A, rows jt + 64q, at
+  // 64q + aE (q even) or 64q + (aE ^ 12) (q odd: g gains bit 2, h flips); B, rows 8 jt + q, at
+  // bB ^ q; C, rows 64u + l + 8q, at (cB ^ ((q >> 1) | ((q & 1) << 3))) + 16 (q >> 1)
+  // (as shared byte addresses; the column starts on a 128-byte boundary, so XOR masks below 128
+  // act on the element index alone)
+  const int l = jt & 7, u = jt >> 3;
+  const uint32_t s32 = smem_u32(s);
+  const uint32_t aE = s32 + 8u * (16 * (u >> 1) + ((l ^ (u >> 1)) | ((u & 1) << 3)));
+  const uint32_t bB = s32 + 8u * (16 * (4 * u + (l >> 1)) + (((l ^ u) & 1) << 3) + ((l >> 1) | ((u & 1) << 2)));
+  const uint32_t cB = s32 + 8u * (64 * u + ((l ^ ((u & 1) << 2)) | ((u & 1) << 3)));
+#define XG_LDA(q) xg_ld<((q) & 1) ? 96 : 0, 512 * (q)>(aE)
+#define XG_STA(q, val) xg_st<((q) & 1) ? 96 : 0, 512 * (q)>(aE, val)
+#define XG_STB(q, val) xg_st<8 * (q), 0>(bB, val)
+#define XG_STC(q, val) xg_st<8 * (((q) >> 1) | (((q) & 1) << 3)), 128 * ((q) >> 1)>(cB, val)
+  const int k1 = l;
   // waits as in k_fz_xmix_reg: a first wait that runs out flags the launch and is followed by a
   // full-bound wait; a thread whose second wait runs out is broken (the lead then issues nothing
   // more) and the group carries on with whatever the buffers hold, all indices data-independent
@@ -686,20 +737,19 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       v[q] = make_float2(A.x - B.y, A.y + B.x);
     }
     dftr<float2, 8, true>(v);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) s[pB + q] = v[q];
+    xg_for<8>([&](auto qc) { constexpr int q = decltype(qc)::value; XG_STB(q, v[q]); });
     xg_bar(gid, GS);
     // stage 1 (span 8)
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      float2 x = s[pA + 68 * q];
+    xg_for<8>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      float2 x = XG_LDA(q);
       if (q > 0 && k1 > 0) {
         float2 w = T1[8 * (q - 1) + k1];
         w.y = -w.y;
         x = cmul(x, w);
       }
       v[q] = x;
-    }
+    });
     dftr<float2, 8, true>(v);
     // the velocity at this thread's outputs x = jt + 64q of both lines, read ahead of the last stage
     float ua[8], ub[8];
@@ -712,20 +762,19 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       }
     }
     xg_bar(gid, GS);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) s[pC + 8 * q + (q >> 1)] = v[q];
+    xg_for<8>([&](auto qc) { constexpr int q = decltype(qc)::value; XG_STC(q, v[q]); });
     xg_bar(gid, GS);
     // stage 2 (span 64): outputs x = jt + 64q, accumulated against the velocity
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      float2 x = s[pA + 68 * q];
+    xg_for<8>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      float2 x = XG_LDA(q);
       if (q > 0) {
         float2 w = T2[GS * (q - 1) + jt];
         w.y = -w.y;
         x = cmul(x, w);
       }
       v[q] = x;
-    }
+    });
     dftr<float2, 8, true>(v);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -737,30 +786,27 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
 #pragma unroll
       for (int q = 0; q < 8; ++q) v[q] = acc[q];
       dftr<float2, 8, false>(v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) s[pB + q] = v[q];
+      xg_for<8>([&](auto qc) { constexpr int q = decltype(qc)::value; XG_STB(q, v[q]); });
       xg_bar(gid, GS);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        float2 x = s[pA + 68 * q];
+      xg_for<8>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        float2 x = XG_LDA(q);
         if (q > 0 && k1 > 0) x = cmul(x, T1[8 * (q - 1) + k1]);
         v[q] = x;
-      }
+      });
       dftr<float2, 8, false>(v);
       xg_bar(gid, GS);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) s[pC + 8 * q + (q >> 1)] = v[q];
+      xg_for<8>([&](auto qc) { constexpr int q = decltype(qc)::value; XG_STC(q, v[q]); });
       xg_bar(gid, GS);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        float2 x = s[pA + 68 * q];
+      xg_for<8>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        float2 x = XG_LDA(q);
         if (q > 0) x = cmul(x, T2[GS * (q - 1) + jt]);
         v[q] = x;
-      }
+      });
       dftr<float2, 8, false>(v);
       xg_bar(gid, GS);   // every stage-2 read of the column is done before it is overwritten
-#pragma unroll
-      for (int q = 0; q < 8; ++q) s[pA + 68 * q] = v[q];   // Z(k), k = jt + 64q
+      xg_for<8>([&](auto qc) { constexpr int q = decltype(qc)::value; XG_STA(q, v[q]); });   // Z(k), k = jt + 64q
       xg_bar(gid, GS);
       const long obase = ((long)b * 3 + c) * a.L;
       const float hs = 0.5f * a.so;
@@ -770,7 +816,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
         if (k < KX) {
           const int e = k == 0 ? 0 : N - k;
           const float2 zk = v[q];
-          const float2 zn = s[e + (e >> 4)];
+          const float2 zn = xg_ld<0, 0>(s32 + 8u * (uint32_t)xg_swz(e));
           out[(obase + la) * KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
           out[(obase + la + 1) * KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
         }
@@ -784,6 +830,10 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
     if (issued1 > 0) mbar_wait_bounded(&bar[1], (uint32_t)((issued1 - 1) & 1), FIT_WAIT_CYCLES / 10);
   }
 }
+#undef XG_LDA
+#undef XG_STA
+#undef XG_STB
+#undef XG_STC
 
 // ---- yfwd --------------------------------------------------------------------------------------
 template <int N>
