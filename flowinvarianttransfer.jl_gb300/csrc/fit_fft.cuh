@@ -2,9 +2,13 @@
 //
 // One CTA transforms a tile of C lines at once. The tile lives in shared memory as
 // [element][column] with an XOR swizzle on the column (element e of column c at
-// e*C + (c ^ (e & (C-1)))), so that both access shapes used here are bank-conflict free:
+// r(e)*C + (c ^ (e & (C-1)))), so that both access shapes used here are bank-conflict free:
 // lanes running along columns (strided passes, every butterfly stage) and lanes running along
-// elements (the x-pass loads/stores of contiguous lines).
+// elements (the x-pass loads/stores of contiguous lines). r(e) = e, except for eight-column tiles,
+// where rows e and e ^ 1 trade places when bit 3 of e is set: with 8-byte elements a 16-lane phase
+// then covers 16 different bank pairs also when its lanes span two rows of equal parity (the first
+// stage's writes of rows 8j + q for two j) or eight rows apart (two runs of a contiguous line). With
+// 16-byte elements (8-lane phases) and with C >= 16 the permutation changes no bank.
 //
 // Stage s of radix r, current span Ns (product of the radices before it), butterfly j:
 //   inputs  x[j + q*N/r] (q < r), twiddled by w^{(j mod Ns) * q * N/(Ns*r)}, w = e^{-+2 pi i/N};
@@ -18,7 +22,11 @@
 
 namespace fit {
 
-FIT_D int swz(int e, int c, int C) { return e * C + (c ^ (e & (C - 1))); }
+// PERM = false keeps r(e) = e for every C (a kernel whose registers cannot afford the two address
+// bases the permutation needs in some stage shapes); a tile must be written and read with one PERM.
+template <bool PERM>
+FIT_D int swzp(int e, int c, int C) { return ((PERM && C == 8) ? e ^ ((e >> 3) & 1) : e) * C + (c ^ (e & (C - 1))); }
+FIT_D int swz(int e, int c, int C) { return swzp<true>(e, c, C); }
 
 // ---- radix-r DFTs in registers; INV selects e^{+2 pi i/r} --------------------------------------
 
@@ -360,7 +368,7 @@ struct CtXTile {
   static constexpr size_t SMEM = (size_t)(E + N) * VB;
 };
 
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS, bool PERM = true>
 __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
   constexpr int MAXB = (EPT + R - 1) / R;
   constexpr int NR = N / R;
@@ -376,7 +384,7 @@ __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
       const int k = j % NS;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
-        V x = s[swz(j + q * NR, c, C)];
+        V x = s[swzp<PERM>(j + q * NR, c, C)];
         if (NS > 1 && q > 0) {
           V w = tw[k * q * TS];
           if (INV) w.y = -w.y;
@@ -397,17 +405,17 @@ __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
       const int k = j % NS;
       const int base = (j / NS) * NS * R + k;
 #pragma unroll
-      for (int q = 0; q < R; ++q) s[swz(base + q * NS, c, C)] = v[i][q];
+      for (int q = 0; q < R; ++q) s[swzp<PERM>(base + q * NS, c, C)] = v[i][q];
     }
   }
   __syncthreads();
 }
 
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, bool PERM = true>
 __device__ __forceinline__ void ct_stages(V* s, const V* tw, int tid) {
   if constexpr (S < ct_nst(N)) {
-    ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S)>(s, tw, tid);
-    ct_stages<V, INV, N, C, NTHR, EPT, S + 1>(s, tw, tid);
+    ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S), PERM>(s, tw, tid);
+    ct_stages<V, INV, N, C, NTHR, EPT, S + 1, PERM>(s, tw, tid);
   }
 }
 
@@ -573,11 +581,11 @@ __global__ void __launch_bounds__(CtXTile<V, N>::NTHR) k_ct_r2c_x(const typename
   }
 }
 
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, int SEND>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, int SEND, bool PERM = true>
 __device__ __forceinline__ void ct_stages_range(V* s, const V* tw, int tid) {
   if constexpr (S < SEND) {
-    ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S)>(s, tw, tid);
-    ct_stages_range<V, INV, N, C, NTHR, EPT, S + 1, SEND>(s, tw, tid);
+    ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S), PERM>(s, tw, tid);
+    ct_stages_range<V, INV, N, C, NTHR, EPT, S + 1, SEND, PERM>(s, tw, tid);
   }
 }
 
@@ -599,7 +607,8 @@ struct CtMap {
 // (each thread only rewrites rows it just read). Callers synchronise before reusing s.
 // LOAD_S: load() reads the tile in s itself; the first stage then waits for every thread's loads
 // before it overwrites s.
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, bool LOAD_S = false, typename LD, typename ST>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, bool LOAD_S = false, bool PERM = true, typename LD,
+          typename ST>
 __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD load, ST store) {
   typedef CtMap<N> MP;
   constexpr int RL = MP::RL, NRL = MP::NRL;
@@ -617,7 +626,7 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
         dftr<V, RL, INV>(v[i]);
         if constexpr (!LOAD_S) {
 #pragma unroll
-          for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+          for (int q = 0; q < RL; ++q) s[swzp<PERM>(j * RL + q, c, C)] = v[i][q];
         }
       }
     }
@@ -629,12 +638,12 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
         if (NB % NTHR == 0 || b < NB) {
           const int c = b % C, j = b / C;
 #pragma unroll
-          for (int q = 0; q < RL; ++q) s[swz(j * RL + q, c, C)] = v[i][q];
+          for (int q = 0; q < RL; ++q) s[swzp<PERM>(j * RL + q, c, C)] = v[i][q];
         }
       }
     }
     __syncthreads();
-    ct_stages_range<V, INV, N, C, NTHR, EPT, 1, MP::NST - 1>(s, tw, tid);
+    ct_stages_range<V, INV, N, C, NTHR, EPT, 1, MP::NST - 1, PERM>(s, tw, tid);
 #pragma unroll
     for (int i = 0; i < MB; ++i) {
       const int b = tid + i * NTHR;
@@ -642,7 +651,7 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
         const int c = b % C, j = b / C;
 #pragma unroll
         for (int q = 0; q < RL; ++q) {
-          V x = s[swz(j + q * NRL, c, C)];
+          V x = s[swzp<PERM>(j + q * NRL, c, C)];
           if (q > 0) {
             V w = tw[j * q];
             if (INV) w.y = -w.y;
@@ -662,18 +671,18 @@ __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD loa
       if (NB % NTHR == 0 || b < NB) {
         const int c = b % C, j = b / C;
 #pragma unroll
-        for (int q = 0; q < RL; ++q) s[swz(j + q * NRL, c, C)] = load(i, q, j + q * NRL, c);
+        for (int q = 0; q < RL; ++q) s[swzp<PERM>(j + q * NRL, c, C)] = load(i, q, j + q * NRL, c);
       }
     }
     __syncthreads();
-    ct_stages<V, INV, N, C, NTHR, EPT, 0>(s, tw, tid);
+    ct_stages<V, INV, N, C, NTHR, EPT, 0, PERM>(s, tw, tid);
 #pragma unroll
     for (int i = 0; i < MB; ++i) {
       const int b = tid + i * NTHR;
       if (NB % NTHR == 0 || b < NB) {
         const int c = b % C, j = b / C;
 #pragma unroll
-        for (int q = 0; q < RL; ++q) store(i, q, j + q * NRL, c, s[swz(j + q * NRL, c, C)]);
+        for (int q = 0; q < RL; ++q) store(i, q, j + q * NRL, c, s[swzp<PERM>(j + q * NRL, c, C)]);
       }
     }
   }

@@ -871,7 +871,9 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(Fz
 // [seg*EPT, seg*EPT + EPT) of pencil column t % C (seg = t / C): a warp covers two rows of all C
 // columns per access (conflict-free under the swizzle), and along a pencil the shell index changes
 // rarely, so each thread keeps a running (shell, sum) pair and flushes it to the block's FP64
-// shared-memory bins only when the shell changes.
+// shared-memory bins only when the shell changes. The tile keeps the unpermuted row layout
+// (swzp<false>): the eight transfer sums live across the three transforms, and the permuted
+// layout's second address bases push the kernel further past 32 registers a thread.
 template <int N>
 __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfwd_bin(FzArgs a, const float2* __restrict__ in,
                                                                         const float2* __restrict__ Ceff,
@@ -898,20 +900,20 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
   for (int c = 0; c < 3; ++c) {
     const long ib = ((long)b * 3 + c) * N;
     __syncthreads();
-    ct_fft_mapped<float2, false, N, C, NT, EPT>(
+    ct_fft_mapped<float2, false, N, C, NT, EPT, false, false>(
         s, tw, tid,
         [&](int, int, int e, int cc) -> float2 {
           const long cl = c0 + cc;
           return (cl < a.P1) ? in[(ib + e) * a.P1 + cl] : make_float2(0.f, 0.f);
         },
-        [&](int, int, int e, int cc, float2 val) { s[swz(e, cc, C)] = val; });
+        [&](int, int, int e, int cc, float2 val) { s[swzp<false>(e, cc, C)] = val; });
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < EPT; ++r) {
       const int e = seg * EPT + r;
       const int f = fz_freq(e, N);
       if (col < a.P1 && f >= -a.K && f <= a.K) {
-        const float2 nv = s[swz(e, mycol, C)];
+        const float2 nv = s[swzp<false>(e, mycol, C)];
         const float2 cv = Ceff[((long)c * a.KY + f + a.K) * a.P1 + col];
         tacc[r] += cv.x * nv.x + cv.y * nv.y;
       }

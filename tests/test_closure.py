@@ -411,7 +411,8 @@ def test_closure_data_matches_oracle():
 def test_learned_closure_gain():
     """Trained on the exact flux of half the domain of an evolved 64^3 field, the network predicts
     Pi_ell on the other half far better than the method without a closure (Pi = 0, relative
-    L2 error 1) and with high correlation."""
+    L2 error 1) and with high correlation; the mixed form (network on the residual over the
+    gradient model) beats the gradient model by at least 7 % in relative L2 error."""
     import torch
     N = 64
     ns = (N, N, N)
@@ -432,9 +433,11 @@ def test_learned_closure_gain():
         assert hist[-1][1] < hist[0][1]
         assert ev["rel_l2_mlp"] < 0.6 * ev["rel_l2_no_closure"]
         assert ev["corr_mlp"] > 0.75
-    # the residual network keeps the gradient model's accuracy and adds to it
+    # the residual network improves on the gradient model by a clear margin (measured: rel L2 0.458
+    # against 0.519, 0.88x; correlation 0.853 against 0.848)
     ev = res[(True, True)]
-    assert ev["rel_l2_mlp"] <= ev["rel_l2_gradient_model"] * 1.02
+    assert ev["rel_l2_mlp"] <= 0.93 * ev["rel_l2_gradient_model"]
+    assert ev["corr_mlp"] >= ev["corr_gradient_model"] - 0.01
 
 
 @pytest.mark.gpu
