@@ -4,11 +4,12 @@
 // [element][column] with an XOR swizzle on the column (element e of column c at
 // r(e)*C + (c ^ (e & (C-1)))), so that both access shapes used here are bank-conflict free:
 // lanes running along columns (strided passes, every butterfly stage) and lanes running along
-// elements (the x-pass loads/stores of contiguous lines). r(e) = e, except for eight-column tiles,
-// where rows e and e ^ 1 trade places when bit 3 of e is set: with 8-byte elements a 16-lane phase
-// then covers 16 different bank pairs also when its lanes span two rows of equal parity (the first
-// stage's writes of rows 8j + q for two j) or eight rows apart (two runs of a contiguous line). With
-// 16-byte elements (8-lane phases) and with C >= 16 the permutation changes no bank.
+// elements (the x-pass loads/stores of contiguous lines). r(e) = e, except for eight-column tiles
+// of the kernels that opt in, where rows e and e ^ 1 trade places when bit 3 of e is set: with
+// 8-byte elements a 16-lane phase then covers 16 different bank pairs also when its lanes span two
+// rows of equal parity (the first stage's writes of rows 8j + q for two j) or eight rows apart (two
+// runs of a contiguous line). With 16-byte elements (8-lane phases) and with C >= 16 the
+// permutation changes no bank.
 //
 // Stage s of radix r, current span Ns (product of the radices before it), butterfly j:
 //   inputs  x[j + q*N/r] (q < r), twiddled by w^{(j mod Ns) * q * N/(Ns*r)}, w = e^{-+2 pi i/N};
@@ -22,11 +23,12 @@
 
 namespace fit {
 
-// PERM = false keeps r(e) = e for every C (a kernel whose registers cannot afford the two address
-// bases the permutation needs in some stage shapes); a tile must be written and read with one PERM.
+// The permutation is opt-in (PERM): it pays in the 512-point strided passes and costs in the 384-
+// and 256-point ones and in kernels whose registers cannot afford the second address base it needs
+// in some stage shapes. A tile must be written and read with one PERM.
 template <bool PERM>
 FIT_D int swzp(int e, int c, int C) { return ((PERM && C == 8) ? e ^ ((e >> 3) & 1) : e) * C + (c ^ (e & (C - 1))); }
-FIT_D int swz(int e, int c, int C) { return swzp<true>(e, c, C); }
+FIT_D int swz(int e, int c, int C) { return swzp<false>(e, c, C); }
 
 // ---- radix-r DFTs in registers; INV selects e^{+2 pi i/r} --------------------------------------
 
@@ -368,7 +370,7 @@ struct CtXTile {
   static constexpr size_t SMEM = (size_t)(E + N) * VB;
 };
 
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS, bool PERM = true>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int R, int NS, bool PERM = false>
 __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
   constexpr int MAXB = (EPT + R - 1) / R;
   constexpr int NR = N / R;
@@ -411,7 +413,7 @@ __device__ __forceinline__ void ct_stage(V* s, const V* tw, int tid) {
   __syncthreads();
 }
 
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, bool PERM = true>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, bool PERM = false>
 __device__ __forceinline__ void ct_stages(V* s, const V* tw, int tid) {
   if constexpr (S < ct_nst(N)) {
     ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S), PERM>(s, tw, tid);
@@ -581,7 +583,7 @@ __global__ void __launch_bounds__(CtXTile<V, N>::NTHR) k_ct_r2c_x(const typename
   }
 }
 
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, int SEND, bool PERM = true>
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, int S, int SEND, bool PERM = false>
 __device__ __forceinline__ void ct_stages_range(V* s, const V* tw, int tid) {
   if constexpr (S < SEND) {
     ct_stage<V, INV, N, C, NTHR, EPT, ct_radix(N, S), ct_span(N, S), PERM>(s, tw, tid);
@@ -607,7 +609,7 @@ struct CtMap {
 // (each thread only rewrites rows it just read). Callers synchronise before reusing s.
 // LOAD_S: load() reads the tile in s itself; the first stage then waits for every thread's loads
 // before it overwrites s.
-template <typename V, bool INV, int N, int C, int NTHR, int EPT, bool LOAD_S = false, bool PERM = true, typename LD,
+template <typename V, bool INV, int N, int C, int NTHR, int EPT, bool LOAD_S = false, bool PERM = false, typename LD,
           typename ST>
 __device__ __forceinline__ void ct_fft_mapped(V* s, const V* tw, int tid, LD load, ST store) {
   typedef CtMap<N> MP;

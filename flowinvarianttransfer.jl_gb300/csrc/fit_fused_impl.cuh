@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv(Fz
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR, EPT = TT::EPT;
   static_assert(C <= 64 && NT * EPT == E, "zinv: tile column must fit the list entry");
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
@@ -129,11 +130,11 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv(Fz
     float2 val = Hc[(long)kz * a.P1 + cc];
     if (v) val = fz_muli(val, kd[kz]);
     const int f = kz - a.K;
-    s[swz(f < 0 ? f + N : f, cc, C)] = val;
+    s[swzp<PM>(f < 0 ? f + N : f, cc, C)] = val;
   }
   __syncthreads();
-  ct_fft_mapped<float2, true, N, C, NT, EPT, true>(
-      s, tw, tid, [&](int, int, int e, int cc) -> float2 { return s[swz(e, cc, C)]; },
+  ct_fft_mapped<float2, true, N, C, NT, EPT, true, PM>(
+      s, tw, tid, [&](int, int, int e, int cc) -> float2 { return s[swzp<PM>(e, cc, C)]; },
       [&](int, int, int e, int cc, float2 val) {
         const long col = c0 + cc;
         if (col < a.P1) ob[(long)e * a.P1 + col] = val;
@@ -147,6 +148,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
   const long obase = ((((long)b * 3 + c) * 3 + j) * N + z) * N;
-  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const int kx = k0 + cc;
@@ -841,6 +843,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(Fz
                                                                     float2* __restrict__ out,
                                                                     const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -853,7 +856,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(Fz
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
   const long obase = (((long)b * 3 + c) * N + z) * a.KY;
-  ct_fft_mapped<float2, false, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, false, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const int kx = k0 + cc;
@@ -950,6 +953,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_bo
                                                                               float2* __restrict__ out,
                                                                               const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -961,7 +965,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_bo
   __syncthreads();
   const float2* Hc = H + ((long)a.hidx[b] * 3 + c) * a.KY * a.P1;
   float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1;
-  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const long col = c0 + cc;
@@ -991,6 +995,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zfwd_st
                                                                                 float2* __restrict__ out,
                                                                                 const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -1002,7 +1007,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zfwd_st
   __syncthreads();
   const float2* ib = in + ((long)b * 3 + c) * N * a.P1;
   float2* ob = out + ((long)b * 3 + c) * a.KY * a.P1;
-  ct_fft_mapped<float2, false, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, false, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const long col = c0 + cc;
@@ -1024,6 +1029,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uz(FzAr
                                                                           float2* __restrict__ out,
                                                                           const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -1035,7 +1041,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uz(FzAr
   __syncthreads();
   const float2* Hc = H + (long)c * a.KY * a.P1;
   float2* oc = out + (long)c * N * a.P1;
-  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const long col = c0 + cc;
@@ -1053,6 +1059,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uy(FzAr
                                                                           float2* __restrict__ out,
                                                                           const float2* __restrict__ twg) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -1064,7 +1071,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uy(FzAr
   __syncthreads();
   const float2* ib = in + ((long)c * N + z) * a.P1;
   float2* ob = out + ((long)c * N + z) * N * a.KX;
-  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const int kx = k0 + cc;
@@ -1082,6 +1089,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_ux(FzAr
                                                                           float* __restrict__ out,
                                                                           const float2* __restrict__ twg, float scale) {
   typedef FzTile<N> TT;
+  constexpr bool PM = N == 512;   // permuted tile rows (see swzp) at 512 points
   constexpr int C = TT::C, E = TT::E, NT = TT::NTHR;
   extern __shared__ __align__(16) unsigned char fit_smem_raw[];
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
@@ -1090,7 +1098,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_ux(FzAr
   const long l0 = (long)blockIdx.x * 2 * C;   // lines of all three components, 2C per block
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
-  ct_fft_mapped<float2, true, N, C, NT, TT::EPT>(
+  ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int k, int col) -> float2 {
         const bool cj = 2 * k > N;
