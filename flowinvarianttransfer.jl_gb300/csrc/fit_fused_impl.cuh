@@ -582,8 +582,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
 // (N = 512), with no block-wide barrier inside the pipeline: each complex column (a pair of lines)
 // belongs to a group of N/8 threads (two warps at N = 512; one radix-8 butterfly per thread and
 // stage) that syncs on its own named barrier and streams its own 2 gradient lines (double buffered)
-// by bulk copies on its own mbarriers; the advecting velocity is read from global memory (L2) into
-// registers ahead of the last inverse stage. The 8 groups of a block share only the twiddle tables,
+// and its 2 velocity lines (single buffered, issued once the step's product has read the previous
+// ones) by bulk copies on its own mbarriers. The 8 groups of a block share only the twiddle tables,
 // so a group never waits for another group's progress.
 // Column layout: row e = 64 e2 + 8 e1 + e0 of a 512-element column sits at
 //   P(e) = 16 (e >> 4) + ((e0 ^ g) | (h << 3)),  g = (e1 >> 1) | ((e2 & 1) << 2),  h = (e1 ^ e2) & 1,
@@ -605,8 +605,9 @@ struct XGTile {
   static constexpr int CP = N;                                       // column length (XOR layout)
   static constexpr size_t OFF_T1 = (size_t)C * CP * 8;
   static constexpr size_t OFF_T2 = OFF_T1 + 7 * 8 * 8;
-  static constexpr size_t OFF_BAR = OFF_T2 + 7 * (size_t)G * 8;      // 2 mbarriers per group
-  static constexpr size_t OFF_G = (OFF_BAR + 2 * C * 8 + 127) / 128 * 128;   // then 2 x C x (2 KX) complex
+  static constexpr size_t OFF_BAR = OFF_T2 + 7 * (size_t)G * 8;      // 3 mbarriers per group
+  static constexpr size_t OFF_U = (OFF_BAR + 3 * C * 8 + 127) / 128 * 128;   // C x 2 velocity lines (floats)
+  static constexpr size_t OFF_G = OFF_U + (size_t)C * 2 * N * 4;     // then 2 x C x (2 KX) complex
 };
 
 FIT_D void xg_bar(int id, int nthr) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthr) : "memory"); }
@@ -662,7 +663,8 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
   float2* s = reinterpret_cast<float2*>(fit_smem_raw) + (size_t)g * TT::CP;      // this group's column
   float2* T1 = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_T1);
   float2* T2 = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_T2);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(fit_smem_raw + TT::OFF_BAR) + 2 * g;   // gradient buffers 0, 1
+  uint64_t* bar = reinterpret_cast<uint64_t*>(fit_smem_raw + TT::OFF_BAR) + 3 * g;   // gradient buffers 0, 1; velocity
+  float* vbuf = reinterpret_cast<float*>(fit_smem_raw + TT::OFF_U) + (size_t)g * 2 * N;   // lines la, la + 1
   const int KX = a.KX;
   float2* gbuf = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_G) + (size_t)g * 2 * (2 * KX);
   const uint32_t gbytes = (uint32_t)(2 * KX) * 8u;
@@ -678,12 +680,15 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
   if (lead) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
     mbar_init_fence();
   }
   __syncthreads();   // the only block-wide barrier: twiddle tables and mbarriers ready
   if (lead) {
     mbar_expect_tx(&bar[0], gbytes);
     bulk_g2s(gbuf, G + (((long)b * 9) * a.L + la) * KX, gbytes, &bar[0]);
+    mbar_expect_tx(&bar[2], 2u * N * 4u);   // velocity lines of step 0 (j = 0), 4 KB contiguous
+    bulk_g2s(vbuf, U + la * N, 2u * N * 4u, &bar[2]);
   }
   // per-thread bases of the three access shapes (l = jt & 7, u = jt >> 3): A, rows jt + 64q, at
   // 64q + aE (q even) or 64q + (aE ^ 12) (q odd: g gains bit 2, h flips); B, rows 8 jt + q, at
@@ -704,7 +709,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
   // full-bound wait; a thread whose second wait runs out is broken (the lead then issues nothing
   // more) and the group carries on with whatever the buffers hold, all indices data-independent
   bool failed = false, broken = false;
-  int issued0 = 1, issued1 = 0;
+  int issued0 = 1, issued1 = 0, issued2 = 1;
   float2 acc[8];
   float2 v[8];
   for (int t = 0; t < 9; ++t) {
@@ -753,16 +758,6 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       v[q] = x;
     });
     dftr<float2, 8, true>(v);
-    // the velocity at this thread's outputs x = jt + 64q of both lines, read ahead of the last stage
-    float ua[8], ub[8];
-    {
-      const float* Ua = U + (long)j * Mtot + la * N + jt;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        ua[q] = __ldg(Ua + NR * q);
-        ub[q] = __ldg(Ua + N + NR * q);
-      }
-    }
     xg_bar(gid, GS);
     xg_for<8>([&](auto qc) { constexpr int q = decltype(qc)::value; XG_STC(q, v[q]); });
     xg_bar(gid, GS);
@@ -778,12 +773,20 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       v[q] = x;
     });
     dftr<float2, 8, true>(v);
+    // the velocity at this thread's outputs x = jt + 64q of both lines, staged by the step's copy
+    if (!mbar_wait_or_flag(&bar[2], (uint32_t)(t & 1), a.wlim, failed)) broken = true;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      acc[q].x += ua[q] * v[q].x;
-      acc[q].y += ub[q] * v[q].y;
+      acc[q].x += vbuf[jt + NR * q] * v[q].x;
+      acc[q].y += vbuf[N + jt + NR * q] * v[q].y;
     }
-    xg_bar(gid, GS);   // the column is free for the next stage-0 writes
+    xg_bar(gid, GS);   // the column and the velocity buffer are free
+    if (lead && t + 1 < 9 && !broken) {   // the next step's velocity lines (read only after this barrier)
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[2], 2u * N * 4u);
+      bulk_g2s(vbuf, U + (long)((t + 1) % 3) * Mtot + la * N, 2u * N * 4u, &bar[2]);
+      ++issued2;
+    }
     if (j == 2) {   // forward transform of the product, kx <= K of both lines
 #pragma unroll
       for (int q = 0; q < 8; ++q) v[q] = acc[q];
@@ -830,6 +833,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
   if (lead) {   // no copy may still be landing when the block exits: the last issued phase of each
     mbar_wait_bounded(&bar[0], (uint32_t)((issued0 - 1) & 1), FIT_WAIT_CYCLES / 10);
     if (issued1 > 0) mbar_wait_bounded(&bar[1], (uint32_t)((issued1 - 1) & 1), FIT_WAIT_CYCLES / 10);
+    mbar_wait_bounded(&bar[2], (uint32_t)((issued2 - 1) & 1), FIT_WAIT_CYCLES / 10);
   }
 }
 #undef XG_LDA
