@@ -54,7 +54,7 @@ def parse():
                     help="1-based mediator shell whose full column the oracle computes for the headline's "
                          "error line (0: skip)")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison")
-    ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial", "padded", "m2m", "band", "frontend", "xpass", "ypass"],
+    ap.add_argument("--config", default="s2s", choices=["s2s", "closure", "batch", "partial", "padded", "m2m", "band", "frontend", "xpass", "ypass", "zbin"],
                     help="s2s: the 512^3 shell-to-shell headline; closure: learned closure vs exact "
                          "coarse-graining flux on a forced 256^3 field; batch: 64 uneven spectral-flux "
                          "instances per graph launch; partial: 512^3 helical partial fluxes of kinetic energy "
@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--lines", type=int, default=65536, help="xpass config: x lines of the one-mediator slice")
     ap.add_argument("--planes", type=int, default=128, help="ypass config: z planes of the one-mediator slice")
+    ap.add_argument("--mediators", type=int, default=1, help="zbin config: mediators of the z-forward + binning pass")
     ap.add_argument("--branches", type=int, default=8, help="batch config: concurrent graph branches")
     ap.add_argument("--closure-n", type=int, default=256)
     ap.add_argument("--closure-nsteps", type=int, default=200)
@@ -1250,9 +1251,11 @@ def run_frontend(args):
 def run_pass(args):
     """One kernel of the fused shell-to-shell pipeline alone on a slice of the 512^3 workload, on
     synthetic device data: the x pass (``--config xpass``, one mediator of full x extent over
-    ``--lines`` x lines, about 2.3 GB at the default 65536; both forms of the kernel) or the
-    y-inverse pass (``--config ypass``, one mediator over ``--planes`` z planes, 4.6 GB). These are
-    the small cases the kernel-level profiles are taken on; the per-unit bytes scale to full launches."""
+    ``--lines`` x lines, about 2.3 GB at the default 65536; both forms of the kernel), the
+    y-inverse pass (``--config ypass``, one mediator over ``--planes`` z planes, 4.6 GB) or the
+    z-forward + binning pass (``--config zbin``, ``--mediators`` mediators over all pencils, 1.2 GB
+    + 0.7 GB per mediator). These are the small cases the kernel-level profiles are taken on; the
+    per-unit bytes scale to full launches."""
     import ctypes as C
     import torch
     import __graft_entry__
@@ -1260,7 +1263,8 @@ def run_pass(args):
     lib = F._lib.load()
     torch.cuda.set_device(0)
     xpass = args.config == "xpass"
-    units = args.lines if xpass else args.planes
+    pass_ = {"xpass": 0, "ypass": 1, "zbin": 2}[args.config]
+    units = {"xpass": args.lines, "ypass": args.planes, "zbin": args.mediators}[args.config]
     forms = (("column_groups", None), ("block_register", "1")) if xpass else (("default", None),)
     out = {}
     for form, env in forms:
@@ -1269,21 +1273,22 @@ def run_pass(args):
         else:
             os.environ.pop("FIT_XMIX_REG", None)
         ms, by = C.c_double(), C.c_double()
-        F._lib.check(lib.fit_bench_fused_pass(0 if xpass else 1, args.n, units, max(1, args.steps), C.byref(ms),
-                                              C.byref(by)))
+        F._lib.check(lib.fit_bench_fused_pass(pass_, args.n, units, max(1, args.steps), C.byref(ms), C.byref(by)))
         out[form] = {"ms": ms.value, "GBps": by.value / (ms.value / 1e3) / 1e9, "alg_bytes": by.value}
     os.environ.pop("FIT_XMIX_REG", None)
     peak, kind = read_peaks()
     head = out[forms[0][0]]
-    what = "x pass" if xpass else "y-inverse pass"
-    slice_ = f"{units} x lines" if xpass else f"{units} z planes"
+    what = {0: "x pass", 1: "y-inverse pass", 2: "z-forward + binning pass"}[pass_]
+    kern = {0: "s2s_xmix", 1: "s2s_yinv", 2: "s2s_zfwd_bin"}[pass_]
+    slice_ = {0: f"one mediator, {units} x lines", 1: f"one mediator, {units} z planes",
+              2: f"{units} mediators, all pencils"}[pass_]
     line = {"metric": f"{args.n}-point {what} of the fused shell-to-shell pipeline: algorithmic GB/s",
             "value": head["GBps"], "unit": "GB/s", "n_gpus": 1, "steps": max(1, args.steps), "warmup": 1,
             "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"one mediator, {slice_} of a {args.n}^3 grid, 2/3 rule, full extent",
+            "config": {"workload": f"{slice_} of a {args.n}^3 grid, 2/3 rule, full extent",
                        "l2": "inputs %.1f GB per launch > 129 MB L2" % (head["alg_bytes"] / 1e9)},
-            "roofline": {"bound": "hbm", "kernel": "s2s_xmix" if xpass else "s2s_yinv", "achieved": head["GBps"],
+            "roofline": {"bound": "hbm", "kernel": kern, "achieved": head["GBps"],
                          "peak": peak, "unit": "GB/s", "frac": head["GBps"] / peak, "peak_source": kind,
                          "algorithmic_bytes_per_launch": head["alg_bytes"], "traffic": None},
             "forms": out}
@@ -1309,7 +1314,7 @@ def main():
         return run_band(args)
     if args.config == "frontend":
         return run_frontend(args)
-    if args.config in ("xpass", "ypass"):
+    if args.config in ("xpass", "ypass", "zbin"):
         return run_pass(args)
     return run_ours(args)
 

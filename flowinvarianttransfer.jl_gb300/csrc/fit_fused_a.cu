@@ -58,7 +58,7 @@ int fz_terms_a(int N, const FzArgs& a, const float2* H, const float* kd, const f
 
 }  // namespace fit
 
-// ---- benchmark hook: the x pass alone on synthetic device data ------------------------------------
+// ---- benchmark hook: one fused pass alone on synthetic device data ----------------------------------
 namespace {
 
 __global__ void k_bench_fill(float* p, long n, unsigned seed) {
@@ -68,6 +68,17 @@ __global__ void k_bench_fill(float* p, long n, unsigned seed) {
     h *= 0x5bd1e995u;
     h ^= h >> 15;
     p[i] = (float)(h & 0xffffff) / 16777216.0f - 0.5f;
+  }
+}
+
+// shell index of live-box mode (kx, f_y, f_z) in shells of width dk (0 beyond the last shell)
+__global__ void k_bench_shells(uint16_t* seff, int K, int KX, long P1, float dk, int nsh) {
+  const long n = (long)(2 * K + 1) * P1;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long col = i % P1;
+    const int kx = (int)(col % KX), fy = (int)(col / KX) - K, fz = (int)(i / P1) - K;
+    const int sh = (int)(sqrtf((float)(kx * kx + fy * fy + fz * fz)) / dk) + 1;
+    seff[i] = (uint16_t)(sh <= nsh ? sh : 0);
   }
 }
 
@@ -83,17 +94,24 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   a.KY = KY;
   a.P1 = P1;
   a.L = pass == 0 ? units : L;
-  a.nsh = 1;
-  a.nb = 1;
-  a.med[0] = 1;
-  a.ext[0][0] = a.ext[0][1] = a.ext[0][2] = (short)K;
+  a.nsh = pass == 2 ? 32 : 1;
+  a.nb = pass == 2 ? (int)units : 1;
+  for (int b = 0; b < a.nb; ++b) {
+    a.med[b] = b + 1;
+    a.ext[b][0] = a.ext[b][1] = a.ext[b][2] = (short)K;
+  }
   a.so = 1.0f / ((float)N * N * N);
   const long Mtot = (long)N * N * N;
   // pass 0 (x pass): G (9 lines x KX per line), U (3 velocity fields, the last one sliced), out (3 x KX);
-  // pass 1 (y inverse): the six z-pass outputs of all N planes in, nine y-pass outputs out
-  const size_t in_n = pass == 0 ? (size_t)9 * units * KX : (size_t)6 * N * P1;
-  const size_t un = pass == 0 ? (size_t)(2 * Mtot + units * (long)N) : (size_t)KY;
-  const size_t on = pass == 0 ? (size_t)3 * units * KX : (size_t)9 * L * KX;
+  // pass 1 (y inverse): the six z-pass outputs of all N planes in, nine y-pass outputs out;
+  // pass 2 (z forward + binning, `units` mediators): their y-forward outputs in (3 x N x P1 each),
+  // the effective carrier (3 x KY x P1, in U's place) and shell ids of 32 shells of width 14 N/512,
+  // block partials out
+  const long pt = (P1 + FzTile<N>::C - 1) / FzTile<N>::C;
+  const size_t in_n = pass == 0 ? (size_t)9 * units * KX : pass == 1 ? (size_t)6 * N * P1 : (size_t)3 * units * N * P1;
+  const size_t un = pass == 0 ? (size_t)(2 * Mtot + units * (long)N) : pass == 1 ? (size_t)KY : (size_t)6 * KY * P1;
+  const size_t on = pass == 0 ? (size_t)3 * units * KX : pass == 1 ? (size_t)9 * L * KX : (size_t)units * 32 * pt;
+  uint16_t* seff = nullptr;
   float2 *in = nullptr, *out = nullptr, *tw = nullptr;
   float* U = nullptr;
   int* err = nullptr;
@@ -114,14 +132,17 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   };
   auto launch = [&]() -> int {
     if (pass == 0) return fz_xpass<N>(a, in, U, out, tw, err, st);
-    return fz_yinv<N>(a, in, U, out, tw, err, (int)units, st);
+    if (pass == 1) return fz_yinv<N>(a, in, U, out, tw, err, (int)units, st);
+    return fz_zfwd_bin<N>(a, in, (const float2*)U, seff, (double*)out, tw, st);
   };
   if (ck(cudaMalloc(&in, in_n * 8)) && ck(cudaMalloc(&U, un * 4)) && ck(cudaMalloc(&out, on * 8)) &&
+      ck(cudaMalloc(&seff, (pass == 2 ? (size_t)KY * P1 : 1) * sizeof(uint16_t))) &&
       ck(cudaMalloc(&tw, (size_t)N * 8)) && ck(cudaMalloc(&err, sizeof(int))) && ck(cudaStreamCreate(&st)) &&
       ck(cudaEventCreate(&e0)) && ck(cudaEventCreate(&e1)) && ck(cudaMemsetAsync(err, 0, sizeof(int), st)) &&
       ck(cudaMemcpyAsync(tw, h.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st))) {
     k_bench_fill<<<1216, 256, 0, st>>>((float*)in, (long)in_n * 2, 1u);
     k_bench_fill<<<1216, 256, 0, st>>>(U, (long)un, 2u);
+    if (pass == 2) k_bench_shells<<<1216, 256, 0, st>>>(seff, K, KX, P1, 14.0f * N / 512.0f, 32);
     rc = launch();   // warm-up (kernel attributes)
     if (rc == FIT_OK && ck(cudaEventRecord(e0, st))) {
       for (int r = 0; r < reps && rc == FIT_OK; ++r) rc = launch();
@@ -129,8 +150,9 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
       if (rc == FIT_OK && ck(cudaEventRecord(e1, st)) && ck(cudaStreamSynchronize(st)) &&
           ck(cudaEventElapsedTime(&t, e0, e1))) {
         *ms = (double)t / reps;
-        *bytes = pass == 0 ? 8.0 * 12.0 * (double)units * KX + 4.0 * 3.0 * (double)N * units
-                           : 8.0 * ((double)units * (6.0 * P1 + 9.0 * (double)N * KX));
+        *bytes = pass == 0   ? 8.0 * 12.0 * (double)units * KX + 4.0 * 3.0 * (double)N * units
+                 : pass == 1 ? 8.0 * ((double)units * (6.0 * P1 + 9.0 * (double)N * KX))
+                             : 8.0 * ((double)units * 3.0 * N * P1 + 3.0 * KY * P1) + 2.0 * KY * P1;
         int hf = 0;
         if (ck(cudaMemcpy(&hf, err, sizeof(int), cudaMemcpyDeviceToHost)) && hf) {
           fit_set_error("fused-pass benchmark: a bounded wait timed out");
@@ -145,6 +167,7 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   cudaFree(out);
   cudaFree(tw);
   cudaFree(err);
+  cudaFree(seff);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (st) cudaStreamDestroy(st);
@@ -155,8 +178,8 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
 
 extern "C" int fit_bench_fused_pass(int pass, int N, long long units, int reps, double* ms_per_launch,
                                     double* alg_bytes) {
-  const long long maxu = pass == 0 ? (long long)N * N : (long long)N;
-  if (!ms_per_launch || !alg_bytes || reps < 1 || (pass != 0 && pass != 1) || units < 1 || units > maxu ||
+  const long long maxu = pass == 0 ? (long long)N * N : pass == 1 ? (long long)N : 8;
+  if (!ms_per_launch || !alg_bytes || reps < 1 || pass < 0 || pass > 2 || units < 1 || units > maxu ||
       (pass == 0 && units % 16 != 0)) {
     fit_set_error("fused-pass benchmark: pass 0 (x lines: a multiple of 16, at most N^2) or 1 (z planes: at "
                   "most N), reps >= 1");

@@ -948,6 +948,20 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
   for (int t = tid; t < a.nsh; t += NT) pb[(long)t * gridDim.z] = bins[t];
 }
 
+// The z-forward + shell-binning pass of a batch: one block per (mediator, pencil tile), block
+// partials to partial[mediator][shell][tile].
+template <int N>
+int fz_zfwd_bin(const FzArgs& a, const float2* in, const float2* Ceff, const uint16_t* seff, double* partial,
+                const float2* tw, cudaStream_t st) {
+  typedef FzTile<N> TT;
+  const size_t smb = TT::SMEM + sizeof(double) * a.nsh + 16;
+  FIT_TRY(ct_prep_fused(k_fz_zfwd_bin<N>, smb, TT::NTHR));
+  const unsigned pt = (unsigned)((a.P1 + TT::C - 1) / TT::C);
+  k_fz_zfwd_bin<N><<<dim3(a.nb, 1, pt), TT::NTHR, smb, st>>>(a, in, Ceff, seff, partial, tw);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 // ---- whole-box terms (partial fluxes) -------------------------------------------------------------
 // z pass of a whole live box (no shell restriction): mediator b transforms field hidx[b] of H and
 // its ik_z derivative; outputs as zinv's.
@@ -1290,12 +1304,10 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   typedef FzTile<N> TT;
   constexpr int C = TT::C;
   const size_t sm = TT::SMEM;
-  const size_t smb = TT::SMEM + sizeof(double) * a.nsh + 16;
   FIT_TRY(ct_prep_fused(k_fz_zinv<N>, sm, TT::NTHR));
   FIT_TRY(ct_prep_fused(k_fz_yinv<N>, sm, TT::NTHR));
   FIT_TRY(ct_prep_fused(k_fz_xmix<N>, sm, TT::NTHR));
   FIT_TRY(ct_prep_fused(k_fz_yfwd<N>, sm, TT::NTHR));
-  FIT_TRY(ct_prep_fused(k_fz_zfwd_bin<N>, smb, TT::NTHR));
   const unsigned pt = (unsigned)((a.P1 + C - 1) / C);
   const unsigned nkt = (unsigned)((a.KX + C - 1) / C);
   const double cpx = 8.0;
@@ -1326,9 +1338,8 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
   fit_prof_end(st);
   FIT_LAUNCH_CHECK();
   fit_prof_begin(PK_S2S_ZFWD_BIN, cpx * (a.nb * 3.0 * N * a.P1 + 3.0 * a.KY * a.P1) + 2.0 * a.KY * a.P1, st);
-  k_fz_zfwd_bin<N><<<dim3(a.nb, 1, pt), TT::NTHR, smb, st>>>(a, bufB, Ceff, seff, partial, tw);
+  FIT_TRY(fz_zfwd_bin<N>(a, bufB, Ceff, seff, partial, tw, st));
   fit_prof_end(st);
-  FIT_LAUNCH_CHECK();
   return FIT_OK;
 }
 

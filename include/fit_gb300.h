@@ -224,13 +224,15 @@ int fit_autotune_info(int64_t* n_entries, int64_t* n_runtime_engine, double* ms_
 int fit_autotune_entry(int64_t i, int64_t* fields, double* ms);
 
 /* Benchmark hook (no counterpart in the reference): times one kernel of the fused shell-to-shell
- * pipeline alone on synthetic device data, one mediator of full extent on an N^3 grid under the
+ * pipeline alone on synthetic device data, mediators of full extent on an N^3 grid under the
  * 2/3 rule, N in {64, 128, 256, 512}; reps launches after one warm-up. pass 0: the x pass (inverse
- * x transforms, product with the advecting velocity, forward x transform) over `units` x lines (a
- * multiple of 16, at most N^2); pass 1: the y-inverse pass over `units` z planes (at most N).
- * ms_per_launch = mean launch time, alg_bytes = the launch's algorithmic bytes. Allocates its
- * buffers for the call and frees them (about 2.3 GB for the x pass at N = 512 over 65536 lines,
- * 4.6 GB for the y pass at N = 512). */
+ * x transforms, product with the advecting velocity, forward x transform) of one mediator over
+ * `units` x lines (a multiple of 16, at most N^2); pass 1: the y-inverse pass of one mediator over
+ * `units` z planes (at most N); pass 2: the z-forward + shell-binning pass of `units` mediators (at
+ * most 8) over all pencils, 32 shells of width 14 N / 512. ms_per_launch = mean launch time,
+ * alg_bytes = the launch's algorithmic bytes. Allocates its buffers for the call and frees them
+ * (at N = 512: about 2.3 GB for the x pass over 65536 lines, 4.6 GB for the y pass, 1.2 GB + 0.7 GB
+ * per mediator for the z pass). */
 int fit_bench_fused_pass(int pass, int N, long long units, int reps, double* ms_per_launch, double* alg_bytes);
 
 /* ---- learned subfilter-stress closure (no counterpart in the reference) -------------------------
