@@ -479,11 +479,53 @@ __global__ void __launch_bounds__(128) k_copy_kept_box(const E* __restrict__ src
   }
 }
 
+// The same copy of 8-byte elements (complex64) in 16-byte pairs, for an even row length and 16-byte
+// aligned arrays (so every row starts on a 16-byte boundary): run A, x in [0, K0], from x = 0 with a
+// single element at its end when its length is odd; run B, x in [N0 - K0, N0), with a single
+// element at its start when N0 - K0 is odd. Each thread issues its first two pairs' loads before
+// any store, so a block keeps up to 256 loads of 16 bytes in flight over the host link.
+__global__ void __launch_bounds__(128) k_copy_kept_box_c64(const uint2* __restrict__ src, uint2* __restrict__ dst,
+                                                           int N0, int N1, int N2, int K0, int K1, int K2) {
+  const int ny = 2 * K1 + 1, nz = 2 * K2 + 1;
+  const long r = blockIdx.x;
+  const int iy = (int)(r % ny), iz = (int)((r / ny) % nz), c = (int)(r / ((long)ny * nz));
+  const int y = iy <= K1 ? iy : N1 - ny + iy, z = iz <= K2 ? iz : N2 - nz + iz;
+  const long base = (((long)c * N2 + z) * N1 + y) * (long)N0;   // even: N0 is even
+  const int pA = (K0 + 1) >> 1;
+  const int sB = N0 - K0, hB = sB & 1;
+  const int pB = (N0 - sB - hB) >> 1;
+  const int np = pA + pB, qB = (sB + hB) >> 1;   // pair index of run B's first pair
+  const uint4* s4 = reinterpret_cast<const uint4*>(src + base);
+  uint4* d4 = reinterpret_cast<uint4*>(dst + base);
+  uint4 v[2];
+  int at[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int t = threadIdx.x + 128 * k;
+    at[k] = t < pA ? t : (t < np ? qB + (t - pA) : -1);
+    if (at[k] >= 0) v[k] = s4[at[k]];
+  }
+  uint2 e0 = make_uint2(0u, 0u);
+  if (threadIdx.x == 0 && ((K0 + 1) & 1)) e0 = src[base + K0];
+  if (threadIdx.x == 1 && hB) e0 = src[base + sB];
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (at[k] >= 0) d4[at[k]] = v[k];
+  if (threadIdx.x == 0 && ((K0 + 1) & 1)) dst[base + K0] = e0;
+  if (threadIdx.x == 1 && hB) dst[base + sB] = e0;
+  for (int t = threadIdx.x + 256; t < np; t += 128) {   // rows longer than 512 pairs of kept elements
+    const int q = t < pA ? t : qB + (t - pA);
+    d4[q] = s4[q];
+  }
+}
+
 int copy_kept_box(const void* src, void* dst, const int* N, int ncomp, int eb, cudaStream_t st) {
   const int K0 = N[0] / 3 - 1, K1 = N[1] / 3 - 1, K2 = N[2] / 3 - 1;
   const long rows = (long)ncomp * (2 * K1 + 1) * (2 * K2 + 1);
   if (rows <= 0 || K0 < 0) return FIT_OK;
-  if (eb == 16)
+  if (eb == 8 && N[0] % 2 == 0 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0)
+    k_copy_kept_box_c64<<<(unsigned)rows, 128, 0, st>>>((const uint2*)src, (uint2*)dst, N[0], N[1], N[2], K0, K1, K2);
+  else if (eb == 16)
     k_copy_kept_box<uint4><<<(unsigned)rows, 128, 0, st>>>((const uint4*)src, (uint4*)dst, N[0], N[1], N[2], K0, K1, K2);
   else
     k_copy_kept_box<uint2><<<(unsigned)rows, 128, 0, st>>>((const uint2*)src, (uint2*)dst, N[0], N[1], N[2], K0, K1, K2);

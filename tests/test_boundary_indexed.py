@@ -64,22 +64,25 @@ def test_set_shell_index_rejects_out_of_range():
         plan.shell_to_shell_indexed(u, 4, 0, F._lib.S2S_PLAIN)
 
 
-@pytest.mark.parametrize("copy_engine", [False, True])
-def test_pinned_host_input_kept_box(copy_engine, monkeypatch):
+@pytest.mark.parametrize("n,copy_engine", [(64, False), (64, True), (96, False)])
+def test_pinned_host_input_kept_box(n, copy_engine, monkeypatch):
     """Host-pointer call of the batched 2/3 form: pinned host memory is read by the device over the
-    host link (only the kept box), or through the copy engines; both match the oracle."""
+    host link (only the kept box, in 16-byte pairs with single elements at odd run ends: 64 has an
+    odd first run, 96 an odd start of the second), or through the copy engines; both match the
+    oracle."""
     torch = pytest.importorskip("torch")
     if copy_engine:
         monkeypatch.setenv("FIT_KEPT_BOX_COPY_ENGINE", "1")
-    u, ks = spectrum_field((64, 64, 64), e_config2, seed=9)
-    pinned = torch.empty((3, 64, 64, 64), dtype=torch.complex64, pin_memory=True)
-    host = np.transpose(pinned.numpy(), (3, 2, 1, 0))     # column-major (64, 64, 64, 3) view
+    ns = (n, n, n)
+    u, ks = spectrum_field(ns, e_config2, seed=9)
+    pinned = torch.empty((3, n, n, n), dtype=torch.complex64, pin_memory=True)
+    host = np.transpose(pinned.numpy(), (3, 2, 1, 0))     # column-major (n, n, n, 3) view
     host[...] = u.astype(np.complex64)
-    plan = Plan((64, 64, 64), 3, 3, "two_thirds", 32, False, ks)
+    plan = Plan(ns, 3, 3, "two_thirds", 32, False, ks)
     _, edges, Tref, _, _ = O.shell_to_shell(host.astype(np.complex128), ks, ("linear", 6.0), "two_thirds")
     before = plan.info()[8]
     for _ in range(3):
         T, _, _ = plan.shell_to_shell(host, edges, 7, 0, 0, F._lib.S2S_BATCHED)
         assert np.max(np.abs(T - Tref)) <= 1e-5 * np.max(np.abs(Tref))
-    K = 64 // 3 - 1
+    K = n // 3 - 1
     assert plan.info()[8] - before == 3 * 3 * (2 * K + 1) ** 3 * 8   # only the kept box travels
