@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <type_traits>
 
 #define FIT_OK 0
 #define FIT_ERR_ARG -1
@@ -31,8 +32,22 @@ template <> struct Scal<float2> { typedef float t; };
 template <> struct Scal<double2> { typedef double t; };
 
 template <typename V> FIT_HD V mkc(typename Scal<V>::t x, typename Scal<V>::t y) { V r; r.x = x; r.y = y; return r; }
-template <typename V> FIT_HD V cadd(V a, V b) { return mkc<V>(a.x + b.x, a.y + b.y); }
-template <typename V> FIT_HD V csub(V a, V b) { return mkc<V>(a.x - b.x, a.y - b.y); }
+// FP32 complex sums on the paired FP32 pipe of compute capability 10.x (one instruction for both
+// parts): a + b as a paired add, a - b as the paired fma(b, -1, a), which rounds once like the
+// scalar subtraction (b * -1 is exact). Each is the scalar operation bit for bit, but the compiler
+// no longer fuses a preceding product into the sum, so transforms differ at FP32 rounding level.
+template <typename V> FIT_HD V cadd(V a, V b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  if constexpr (std::is_same<V, float2>::value) return __fadd2_rn(a, b);
+#endif
+  return mkc<V>(a.x + b.x, a.y + b.y);
+}
+template <typename V> FIT_HD V csub(V a, V b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  if constexpr (std::is_same<V, float2>::value) return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+#endif
+  return mkc<V>(a.x - b.x, a.y - b.y);
+}
 template <typename V> FIT_HD V cmul(V a, V b) { return mkc<V>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 template <typename V> FIT_HD V cconj(V a) { return mkc<V>(a.x, -a.y); }
 template <typename V, typename S> FIT_HD V cscale(V a, S s) { return mkc<V>(a.x * s, a.y * s); }

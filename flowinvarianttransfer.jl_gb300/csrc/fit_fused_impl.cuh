@@ -535,9 +535,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           if (!mbar_wait_or_flag(&bar[2], (uint32_t)(t & 1), a.wlim, failed)) broken = true;
           return true;
         },
-        [&](int i, int q, int x, int col, float2 zv) {
-          acc[i][q].x += us[col * TT::UP + x] * zv.x;
-          acc[i][q].y += us[(col + C) * TT::UP + x] * zv.y;
+        [&](int i, int q, int x, int col, float2 zv) {   // one paired fma for both lines
+          acc[i][q] = __ffma2_rn(make_float2(us[col * TT::UP + x], us[(col + C) * TT::UP + x]), zv, acc[i][q]);
         });
     __syncthreads();   // s and the velocity tile are free
     if (tid == 0 && t + 1 < 9 && !broken) {   // once broken, issue nothing more
@@ -776,10 +775,8 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
     // the velocity at this thread's outputs x = jt + 64q of both lines, staged by the step's copy
     if (!mbar_wait_or_flag(&bar[2], (uint32_t)(t & 1), a.wlim, failed)) broken = true;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      acc[q].x += vbuf[jt + NR * q] * v[q].x;
-      acc[q].y += vbuf[N + jt + NR * q] * v[q].y;
-    }
+    for (int q = 0; q < 8; ++q)   // (acc.x, acc.y) += (u(la), u(la + 1)) * (v.x, v.y): one paired fma
+      acc[q] = __ffma2_rn(make_float2(vbuf[jt + NR * q], vbuf[N + jt + NR * q]), v[q], acc[q]);
     xg_bar(gid, GS);   // the column and the velocity buffer are free
     if (lead && t + 1 < 9 && !broken) {   // the next step's velocity lines (read only after this barrier)
       fence_proxy_async_smem();

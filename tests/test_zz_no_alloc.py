@@ -5,9 +5,9 @@ latency-critical loop, an embedding runtime lending only its own buffers) use th
 variant; it must give the same S(k|p) and net(k) as the allocating entry point, on consecutive
 calls that reuse its fixed scratch array. FP64 products: within 1e-12 relative (max-norm);
 FP32 products: within 1e-5 relative. Cases: ComplexF64 and ComplexF32 inputs, NoDealiasing and
-the 2/3 rule, a passive scalar advected by a separate velocity, and a 32^3 three-component grid
-at the 32768-mode limit, where the scratch layout is fullest. This file is collected last on
-purpose.
+the 2/3 rule, a passive scalar advected by a separate velocity, a 32^3 three-component grid
+at the 32768-mode limit, where the scratch layout is fullest, and a call captured into a CUDA
+graph and replayed. This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -117,6 +117,38 @@ def test_no_alloc_at_the_mode_limit():
         assert float((net - net_ref).abs().max()) <= 1e-10 * scale
     del S, S_ref
     torch.cuda.empty_cache()
+
+
+def test_no_alloc_captured_in_a_cuda_graph():
+    """After one eager call, a call on a stream under capture enqueues its kernels without
+    synchronising (the capture stays valid); replaying the graph reproduces the eager S and net."""
+    import torch
+    lib, fn = _entry()
+    u, ks = curl_noise_3d(8, 7)
+    u = np.asfortranarray(u.astype(np.complex128))
+    nm = 8 ** 3
+    u_d = _dev(u)
+    ks_d, ks_arr = _ks_dev(ks)
+    nsv = (C.c_int64 * 3)(8, 8, 8)
+    S = torch.full((nm * nm,), float("nan"), dtype=torch.float64, device="cuda")
+    net = torch.full((nm,), float("nan"), dtype=torch.float64, device="cuda")
+    args = (3, nsv, 3, 3, 1, ks_arr, 2, 1, 1, C.c_void_p(u_d.data_ptr()), None, C.c_void_p(S.data_ptr()),
+            C.c_void_p(net.data_ptr()))
+    assert fn(*args, None) == 0, lib.fit_last_error()
+    S_ref, net_ref = S.clone(), net.clone()
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+        rc = fn(*args, C.c_void_p(side.cuda_stream))
+    assert rc == 0, lib.fit_last_error()
+    S.fill_(float("nan"))
+    net.fill_(float("nan"))
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    scale = float(S_ref.abs().max())
+    assert float((S - S_ref).abs().max()) <= 1e-14 * scale
+    assert float((net - net_ref).abs().max()) <= 1e-12 * scale
 
 
 def test_no_alloc_rejects_grids_above_the_limit():
