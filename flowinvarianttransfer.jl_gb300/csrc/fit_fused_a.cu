@@ -93,6 +93,7 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   a.KX = KX;
   a.KY = KY;
   a.P1 = P1;
+  fz_set_strides(&a);
   a.L = pass == 0 ? units : L;
   a.nsh = pass == 2 ? 32 : 1;
   a.nb = pass == 2 ? (int)units : 1;
@@ -108,9 +109,10 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   // the effective carrier (3 x KY x P1, in U's place) and shell ids of 32 shells of width 14 N/512,
   // block partials out
   const long pt = (P1 + FzTile<N>::C - 1) / FzTile<N>::C;
-  const size_t in_n = pass == 0 ? (size_t)9 * units * KX : pass == 1 ? (size_t)6 * N * P1 : (size_t)3 * units * N * P1;
+  const size_t in_n = pass == 0 ? (size_t)9 * units * a.KXS : pass == 1 ? (size_t)6 * N * a.P1S
+                                                                         : (size_t)3 * units * N * a.P1S;
   const size_t un = pass == 0 ? (size_t)(2 * Mtot + units * (long)N) : pass == 1 ? (size_t)KY : (size_t)6 * KY * P1;
-  const size_t on = pass == 0 ? (size_t)3 * units * KX : pass == 1 ? (size_t)9 * L * KX : (size_t)units * 32 * pt;
+  const size_t on = pass == 0 ? (size_t)3 * units * a.KXS : pass == 1 ? (size_t)9 * L * a.KXS : (size_t)units * 32 * pt;
   uint16_t* seff = nullptr;
   float2 *in = nullptr, *out = nullptr, *tw = nullptr;
   float* U = nullptr;

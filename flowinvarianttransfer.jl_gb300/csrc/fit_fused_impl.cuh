@@ -39,6 +39,12 @@ struct FzArgs {
   int K, KX, KY;
   long P1;      // KX * KY live pencils
   long L;       // N * N lines of the x pass
+  // padded row strides of the batch intermediates (multiples of 4 elements, so that every row and
+  // every 8-element tile row segment starts on a 32-byte sector): KXS for the [..][line][kx] arrays
+  // (y-inverse output = x-pass input, x-pass output = y-forward input), P1S for the [..][z][pencil]
+  // arrays (z-inverse output = y-inverse input, y-forward output = z-forward input)
+  int KXS;
+  long P1S;
   int nsh;
   int nb;       // mediators in this launch
   int med[16];  // their shell numbers (1-based)
@@ -60,6 +66,12 @@ struct FzArgs {
   int widx[16];
   long long wlim;   // first bound of the x pass's copy waits (fit_wait_cycles)
 };
+
+// the padded row strides of a batch's intermediates, from its KX and P1
+inline void fz_set_strides(FzArgs* a) {
+  a->KXS = (a->KX + 3) & ~3;
+  a->P1S = (a->P1 + 3) & ~3L;
+}
 
 FIT_D int fz_freq(int e, int N) { return (2 * e <= N) ? e : e - N; }
 FIT_D float2 fz_muli(float2 h, float k) { return make_float2(-h.y * k, h.x * k); }   // i*k*h
@@ -111,11 +123,11 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv(Fz
   if (!live) return;
   const long tl = (long)(m - 1) * a.ntile + tile;
   const unsigned e0 = a.zoff[tl], e1 = a.zoff[tl + 1];
-  float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1;
+  float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1S;
   if (e0 == e1) {   // no mode of the shell in these pencils: the transform is zero
     for (int i = tid; i < E; i += NT) {
       const int cc = i % C, e = i / C;
-      if (c0 + cc < a.P1) ob[(long)e * a.P1 + c0 + cc] = make_float2(0.f, 0.f);
+      if (c0 + cc < a.P1) ob[(long)e * a.P1S + c0 + cc] = make_float2(0.f, 0.f);
     }
     return;
   }
@@ -137,7 +149,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv(Fz
       s, tw, tid, [&](int, int, int e, int cc) -> float2 { return s[swzp<PM>(e, cc, C)]; },
       [&](int, int, int e, int cc, float2 val) {
         const long col = c0 + cc;
-        if (col < a.P1) ob[(long)e * a.P1 + col] = val;
+        if (col < a.P1) ob[(long)e * a.P1S + col] = val;
       });
 }
 
@@ -160,7 +172,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
   const int v = (j == 2) ? 1 : 0;
   const int ex = a.ext[b][0], ey = a.ext[b][1];
   if (k0 > ex) return;   // no mode of the mediator's shell at these kx (outputs never read)
-  const long ib = ((((long)b * 3 + c) * 2 + v) * N + z) * a.P1;
+  const long ib = ((((long)b * 3 + c) * 2 + v) * N + z) * a.P1S;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
   const long obase = ((((long)b * 3 + c) * 3 + j) * N + z) * N;
@@ -180,7 +192,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
       },
       [&](int, int, int e, int cc, float2 val) {
         const int kx = k0 + cc;
-        if (kx < a.KX) out[(obase + e) * a.KX + kx] = val;
+        if (kx < a.KX) out[(obase + e) * a.KXS + kx] = val;
       });
 }
 
@@ -232,8 +244,8 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const flo
         const int kk = cj ? N - k : k;
         float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
         if (kk <= ex) {
-          if (la < a.L) A = G[(gb + la) * a.KX + kk];
-          if (lb < a.L) B = G[(gb + lb) * a.KX + kk];
+          if (la < a.L) A = G[(gb + la) * a.KXS + kk];
+          if (lb < a.L) B = G[(gb + lb) * a.KXS + kk];
           if (cj) { A.y = -A.y; B.y = -B.y; }
           if (k == 0) { A.y = 0.f; B.y = 0.f; }
         }
@@ -270,8 +282,8 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR) k_fz_xmix(FzArgs a, const flo
       const long la = l0 + 2 * col, lb = la + 1;
       const float2 zk = s[swz(k, col, C)];
       const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
-      if (la < a.L) out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
-      if (lb < a.L) out[(obase + lb) * a.KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+      if (la < a.L) out[(obase + la) * a.KXS + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+      if (lb < a.L) out[(obase + lb) * a.KXS + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
     }
   }
 }
@@ -306,7 +318,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
   float2* tw = s + E;
   uint64_t* bar = reinterpret_cast<uint64_t*>(tw + N);
   float2* stg = reinterpret_cast<float2*>(fit_smem_raw + TT::SMEM_FIXED);
-  const int SB = 2 * C * a.KX;
+  const int SB = 2 * C * a.KXS;
   const uint32_t bytes = (uint32_t)SB * 8u;
   const int tid = threadIdx.x;
   const long l0 = (long)blockIdx.z * 2 * C;
@@ -324,7 +336,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
   if (tid == 0) {
     const long gb = ((long)b * 3 * 3) * a.L;
     mbar_expect_tx(&bar[0], bytes);
-    bulk_g2s(stg, G + (gb + l0) * a.KX, bytes, &bar[0]);
+    bulk_g2s(stg, G + (gb + l0) * a.KXS, bytes, &bar[0]);
   }
   float2 acc[EPT];
   bool failed = false;   // a first wait ran out (the second, full-bound wait then succeeded)
@@ -339,7 +351,7 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
       const long gb = (((long)b * 3 + c1) * 3 + j1) * a.L;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[nb1], bytes);
-      bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KX, bytes, &bar[nb1]);
+      bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KXS, bytes, &bar[nb1]);
     }
     // advecting velocity at this thread's accumulate positions (lanes along x: coalesced), loaded
     // ahead of the transform so the loads overlap it
@@ -371,8 +383,8 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
           const int kk = cj ? N - k : k;
           float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
           if (kk <= ex) {
-            A = sg[(2 * col) * a.KX + kk];
-            B = sg[(2 * col + 1) * a.KX + kk];
+            A = sg[(2 * col) * a.KXS + kk];
+            B = sg[(2 * col + 1) * a.KXS + kk];
             if (cj) { A.y = -A.y; B.y = -B.y; }
             if (k == 0) { A.y = 0.f; B.y = 0.f; }
           }
@@ -405,8 +417,8 @@ __global__ void __launch_bounds__(XTile<N>::NTHR, 2) k_fz_xmix_bulk(FzArgs a, co
         const long la = l0 + 2 * col, lb = la + 1;
         const float2 zk = s[swz(k, col, C)];
         const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
-        out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
-        out[(obase + lb) * a.KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+        out[(obase + la) * a.KXS + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+        out[(obase + lb) * a.KXS + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
       }
       __syncthreads();
     }
@@ -457,7 +469,7 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
   uint64_t* bar = reinterpret_cast<uint64_t*>(tw + N);   // [0],[1] gradient buffers, [2] velocity
   float* us = reinterpret_cast<float*>(fit_smem_raw + TT::OFF_U);
   float2* stg = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_G);
-  const int SB = 2 * C * a.KX;
+  const int SB = 2 * C * a.KXS;
   const uint32_t gbytes = (uint32_t)SB * 8u;
   const int tid = threadIdx.x;
   const long l0 = (long)blockIdx.z * 2 * C;
@@ -481,7 +493,7 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
   if (tid == 0) {
     const long gb = ((long)b * 3 * 3) * a.L;
     mbar_expect_tx(&bar[0], gbytes);
-    bulk_g2s(stg, G + (gb + l0) * a.KX, gbytes, &bar[0]);
+    bulk_g2s(stg, G + (gb + l0) * a.KXS, gbytes, &bar[0]);
     mbar_expect_tx(&bar[2], (uint32_t)(2 * C * N * 4));
     for (int r = 0; r < 2 * C; ++r) bulk_g2s(us + urow(r) * TT::UP, U + (l0 + r) * N, (uint32_t)(N * 4), &bar[2]);
   }
@@ -510,7 +522,7 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
       const long gb = (((long)b * 3 + c1) * 3 + j1) * a.L;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[nb1], gbytes);
-      bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KX, gbytes, &bar[nb1]);
+      bulk_g2s(stg + nb1 * SB, G + (gb + l0) * a.KXS, gbytes, &bar[nb1]);
       if (nb1) ++issued1;
       else ++issued0;
     }
@@ -524,8 +536,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
           float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
           if (kk <= ex) {
             const int ra = xp ? col : 2 * col, rb = xp ? col + C : 2 * col + 1;
-            A = sg[ra * a.KX + kk];
-            B = sg[rb * a.KX + kk];
+            A = sg[ra * a.KXS + kk];
+            B = sg[rb * a.KXS + kk];
             if (cj) { A.y = -A.y; B.y = -B.y; }
             if (k == 0) { A.y = 0.f; B.y = 0.f; }
           }
@@ -562,8 +574,8 @@ __global__ void __launch_bounds__(XRTile<N>::NTHR, 2) k_fz_xmix_reg(FzArgs a, co
         const long la = l0 + (xp ? col : 2 * col), lb = la + (xp ? C : 1);
         const float2 zk = s[swz(k, col, C)];
         const float2 zn = s[swz(k == 0 ? 0 : N - k, col, C)];
-        out[(obase + la) * a.KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
-        out[(obase + lb) * a.KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+        out[(obase + la) * a.KXS + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+        out[(obase + lb) * a.KXS + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
       }
       __syncthreads();
     }
@@ -664,9 +676,9 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
   float2* T2 = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_T2);
   uint64_t* bar = reinterpret_cast<uint64_t*>(fit_smem_raw + TT::OFF_BAR) + 3 * g;   // gradient buffers 0, 1; velocity
   float* vbuf = reinterpret_cast<float*>(fit_smem_raw + TT::OFF_U) + (size_t)g * 2 * N;   // lines la, la + 1
-  const int KX = a.KX;
-  float2* gbuf = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_G) + (size_t)g * 2 * (2 * KX);
-  const uint32_t gbytes = (uint32_t)(2 * KX) * 8u;
+  const int KX = a.KX, KXS = a.KXS;
+  float2* gbuf = reinterpret_cast<float2*>(fit_smem_raw + TT::OFF_G) + (size_t)g * 2 * (2 * KXS);
+  const uint32_t gbytes = (uint32_t)(2 * KXS) * 8u;
   const int b = blockIdx.x;
   const int ex = a.ext[b][0];
   const long Mtot = (long)N * N * N;
@@ -685,7 +697,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
   __syncthreads();   // the only block-wide barrier: twiddle tables and mbarriers ready
   if (lead) {
     mbar_expect_tx(&bar[0], gbytes);
-    bulk_g2s(gbuf, G + (((long)b * 9) * a.L + la) * KX, gbytes, &bar[0]);
+    bulk_g2s(gbuf, G + (((long)b * 9) * a.L + la) * KXS, gbytes, &bar[0]);
     mbar_expect_tx(&bar[2], 2u * N * 4u);   // velocity lines of step 0 (j = 0), 4 KB contiguous
     bulk_g2s(vbuf, U + la * N, 2u * N * 4u, &bar[2]);
   }
@@ -721,13 +733,13 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       const int c1 = (t + 1) / 3, j1 = (t + 1) % 3, nb1 = (t + 1) & 1;
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[nb1], gbytes);
-      bulk_g2s(gbuf + nb1 * (2 * KX), G + ((((long)b * 3 + c1) * 3 + j1) * a.L + la) * KX, gbytes, &bar[nb1]);
+      bulk_g2s(gbuf + nb1 * (2 * KXS), G + ((((long)b * 3 + c1) * 3 + j1) * a.L + la) * KXS, gbytes, &bar[nb1]);
       if (nb1) ++issued1;
       else ++issued0;
     }
     if (!mbar_wait_or_flag(&bar[buf], (uint32_t)((t >> 1) & 1), a.wlim, failed)) broken = true;
     // stage 0 of the inverse transform: inputs k = jt + 64q of the Hermitian pair z = A + iB
-    const float2* ga = gbuf + buf * (2 * KX);
+    const float2* ga = gbuf + buf * (2 * KXS);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = jt + NR * q;
@@ -736,7 +748,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
       if (kk <= ex) {
         A = ga[kk];
-        B = ga[KX + kk];
+        B = ga[KXS + kk];
         if (cj) { A.y = -A.y; B.y = -B.y; }
         if (k == 0) { A.y = 0.f; B.y = 0.f; }
       }
@@ -819,8 +831,8 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
           const int e = k == 0 ? 0 : N - k;
           const float2 zk = v[q];
           const float2 zn = xg_ld<0, 0>(s32 + 8u * (uint32_t)xg_swz(e));
-          out[(obase + la) * KX + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
-          out[(obase + la + 1) * KX + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
+          out[(obase + la) * KXS + k] = make_float2((zk.x + zn.x) * hs, (zk.y - zn.y) * hs);
+          out[(obase + la + 1) * KXS + k] = make_float2((zk.y + zn.y) * hs, (zn.x - zk.x) * hs);
         }
       }
       xg_bar(gid, GS);   // the column is free for the next transform
@@ -856,17 +868,17 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(Fz
   const long ib = ((long)b * 3 + c) * a.L + (long)N * z;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
-  const long obase = (((long)b * 3 + c) * N + z) * a.KY;
+  const long obase = (((long)b * 3 + c) * N + z) * a.P1S;
   ct_fft_mapped<float2, false, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const int kx = k0 + cc;
-        return (kx < a.KX) ? in[(ib + e) * a.KX + kx] : make_float2(0.f, 0.f);
+        return (kx < a.KX) ? in[(ib + e) * a.KXS + kx] : make_float2(0.f, 0.f);
       },
       [&](int, int, int e, int cc, float2 val) {
         const int kx = k0 + cc;
         const int f = fz_freq(e, N);
-        if (kx < a.KX && f >= -a.K && f <= a.K) out[(obase + f + a.K) * a.KX + kx] = val;
+        if (kx < a.KX && f >= -a.K && f <= a.K) out[obase + (long)(f + a.K) * a.KX + kx] = val;
       });
 }
 
@@ -908,7 +920,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
         s, tw, tid,
         [&](int, int, int e, int cc) -> float2 {
           const long cl = c0 + cc;
-          return (cl < a.P1) ? in[(ib + e) * a.P1 + cl] : make_float2(0.f, 0.f);
+          return (cl < a.P1) ? in[(ib + e) * a.P1S + cl] : make_float2(0.f, 0.f);
         },
         [&](int, int, int e, int cc, float2 val) { s[swzp<false>(e, cc, C)] = val; });
     __syncthreads();
@@ -979,7 +991,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_bo
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
   const float2* Hc = H + ((long)a.hidx[b] * 3 + c) * a.KY * a.P1;
-  float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1;
+  float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1S;
   ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
@@ -1000,7 +1012,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_bo
       },
       [&](int, int, int e, int cc, float2 val) {
         const long col = c0 + cc;
-        if (col < a.P1) ob[(long)e * a.P1 + col] = val;
+        if (col < a.P1) ob[(long)e * a.P1S + col] = val;
       });
 }
 
@@ -1020,13 +1032,13 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zfwd_st
   const int c = blockIdx.y, b = blockIdx.x;
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
   __syncthreads();
-  const float2* ib = in + ((long)b * 3 + c) * N * a.P1;
+  const float2* ib = in + ((long)b * 3 + c) * N * a.P1S;
   float2* ob = out + ((long)b * 3 + c) * a.KY * a.P1;
   ct_fft_mapped<float2, false, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int e, int cc) -> float2 {
         const long col = c0 + cc;
-        return (col < a.P1) ? ib[(long)e * a.P1 + col] : make_float2(0.f, 0.f);
+        return (col < a.P1) ? ib[(long)e * a.P1S + col] : make_float2(0.f, 0.f);
       },
       [&](int, int, int e, int cc, float2 val) {
         const long col = c0 + cc;
@@ -1153,7 +1165,7 @@ static int ct_prep_fused(K kern, size_t smem, int nthr) {
 }
 
 // Line pairing of the x pass with the fewer shared-memory bank conflicts on the gradient tile:
-// a half-warp reads 8-byte elements at rows row(c) of stride KX for its columns c = lane % C and
+// a half-warp reads 8-byte elements at rows row(c) of stride KX (the tile's row stride, KXS) for its columns c = lane % C and
 // consecutive positions lane / C; the busiest bank's distinct-word count is compared.
 static int fz_xpair(int KX, int C) {
   int best = 0, best_hits = 1 << 30;
@@ -1215,10 +1227,10 @@ int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, cons
   typedef FzTile<N> TT;
   constexpr int C = TT::C;
   typedef XTile<N> XT;
-  const size_t smx = XT::SMEM_FIXED + 2 * (size_t)(2 * XT::C * a.KX) * 8;
+  const size_t smx = XT::SMEM_FIXED + 2 * (size_t)(2 * XT::C * a.KXS) * 8;
   const bool bulk = smx <= 227 * 1024 && (a.L % (2 * XT::C)) == 0;   // 16-byte alignment holds: L, 2C are multiples of 16
   typedef XRTile<N> XR;
-  const size_t smr = XR::OFF_G + 2 * (size_t)(2 * XR::C * a.KX) * 8;
+  const size_t smr = XR::OFF_G + 2 * (size_t)(2 * XR::C * a.KXS) * 8;
   const char* env = getenv("FIT_XMIX_BULK");   // selects the previous form of the x pass
   bool reg = XR::OK && bulk && smr <= 227 * 1024 && !(env && env[0] == '1');
   FzArgs aw = a;
@@ -1226,7 +1238,7 @@ int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, cons
   typedef XGTile<N> XG;
   const char* envr = getenv("FIT_XMIX_REG");   // selects the block-synchronous register form
   if constexpr (XG::OK) {
-    const size_t smg = XG::OFF_G + 2 * (size_t)XG::C * (2 * a.KX) * 8;
+    const size_t smg = XG::OFF_G + 2 * (size_t)XG::C * (2 * a.KXS) * 8;
     if (reg && !(envr && envr[0] == '1') && smg <= 227 * 1024 && (a.L % (2 * XG::C)) == 0) {
       FIT_TRY(ct_prep_fused(k_fz_xmix_grp<N>, smg, XG::NTHR));
       k_fz_xmix_grp<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XG::C))), XG::NTHR, smg, st>>>(aw, G, U, out, tw, err);
@@ -1238,7 +1250,7 @@ int fz_xpass(const FzArgs& a, const float2* G, const float* U, float2* out, cons
     if (reg) {
       FIT_TRY(ct_prep_fused(k_fz_xmix_reg<N>, smr, XR::NTHR));
       FzArgs ax = aw;
-      ax.xpair = fz_xpair(a.KX, XR::C);
+      ax.xpair = fz_xpair(a.KXS, XR::C);
       k_fz_xmix_reg<N><<<dim3(a.nb, 1, (unsigned)(a.L / (2 * XR::C))), XR::NTHR, smr, st>>>(ax, G, U, out, tw, err);
     }
   }

@@ -145,8 +145,8 @@ static int run_partial_box(fit_plan* p, PartialState* s, const void* ud, int dec
   fz_box_dims(p, &a);
   const long BL = (long)a.KY * a.P1;   // live-box modes per field
   const double M = g.M[0];
-  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
-  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  const double perA = 6.0 * M * a.P1S > 3.0 * a.L * a.KXS ? 6.0 * M * a.P1S : 3.0 * a.L * a.KXS;
+  const double perB = 9.0 * a.L * a.KXS > 3.0 * M * a.P1S ? 9.0 * a.L * a.KXS : 3.0 * M * a.P1S;
   FIT_TRY(pbuf(p, &s->bH, sizeof(float2) * 6 * BL));
   FIT_TRY(pbuf(p, &s->bC, sizeof(float2) * 3 * BL * 2 * ninv));
   FIT_TRY(pbuf(p, &s->bse, sizeof(uint16_t) * BL));

@@ -361,6 +361,7 @@ void fz_box_dims(const fit_plan* p, FzArgs* a) {
   a->KX = a->K + 1;
   a->KY = 2 * a->K + 1;
   a->P1 = (long)a->KX * a->KY;
+  fz_set_strides(a);
   a->L = (long)g.M[0] * g.M[0];
   a->nsh = p->nsh;
   a->so = (float)(g.padded ? (double)g.Mtot / ((double)g.Ntot * (double)g.Ntot) : 1.0 / (double)g.Ntot);
@@ -429,8 +430,9 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   const long P1 = (long)KX * KY, L = (long)M * M;
   const int C = fz_tile_cols_a(M) > 0 ? fz_tile_cols_a(M) : fz_tile_cols_b(M);
   const long npt = (P1 + C - 1) / C;
-  const double perA = (double)(6.0 * M * P1 > 3.0 * L * KX ? 6.0 * M * P1 : 3.0 * L * KX);
-  const double perB = (double)(9.0 * L * KX > 3.0 * M * P1 ? 9.0 * L * KX : 3.0 * M * P1);
+  const long KXS = (KX + 3) & ~3, P1S = (P1 + 3) & ~3L;   // the padded row strides (fz_set_strides)
+  const double perA = (double)(6.0 * M * P1S > 3.0 * L * KXS ? 6.0 * M * P1S : 3.0 * L * KXS);
+  const double perB = (double)(9.0 * L * KXS > 3.0 * M * P1S ? 9.0 * L * KXS : 3.0 * M * P1S);
   std::vector<int> meds;   // mediators with at least one mode
   for (int m = 1; m <= nsh; ++m)
     if (s->occ[m - 1] > 0) meds.push_back(m);
@@ -506,6 +508,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   a.KX = KX;
   a.KY = KY;
   a.P1 = P1;
+  fz_set_strides(&a);
   a.L = L;
   a.nsh = nsh;
   a.so = (float)(g.padded ? (double)g.Mtot / ((double)g.Ntot * (double)g.Ntot) : 1.0 / (double)g.Ntot);
@@ -576,8 +579,8 @@ int s2s_box_flux(fit_plan* p, const void* ud, const void* ad, const void* cd, in
   fz_box_dims(p, &a);
   const long BL = (long)a.KY * a.P1;
   const double M = g.M[0];
-  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
-  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  const double perA = 6.0 * M * a.P1S > 3.0 * a.L * a.KXS ? 6.0 * M * a.P1S : 3.0 * a.L * a.KXS;
+  const double perB = 9.0 * a.L * a.KXS > 3.0 * M * a.P1S ? 9.0 * a.L * a.KXS : 3.0 * M * a.P1S;
   FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 6 * BL));
   FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * BL));
   FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * BL));
@@ -666,8 +669,8 @@ int s2s_box_nonlinear_full(fit_plan* p, const void* ud, void* Nfull) {
   fz_box_dims(p, &a);
   const long BL = (long)a.KY * a.P1;
   const double M = g.M[0];
-  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
-  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  const double perA = 6.0 * M * a.P1S > 3.0 * a.L * a.KXS ? 6.0 * M * a.P1S : 3.0 * a.L * a.KXS;
+  const double perB = 9.0 * a.L * a.KXS > 3.0 * M * a.P1S ? 9.0 * a.L * a.KXS : 3.0 * M * a.P1S;
   FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 3 * BL));
   FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * BL));
   FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * BL));
@@ -806,8 +809,8 @@ int s2s_box_bands(fit_plan* p, const void* ud, const void* ad, int nbands, int i
   fz_box_dims(p, &a);
   const long BL = (long)a.KY * a.P1;
   const double M = g.M[0];
-  const double perA = 6.0 * M * a.P1 > 3.0 * a.L * a.KX ? 6.0 * M * a.P1 : 3.0 * a.L * a.KX;
-  const double perB = 9.0 * a.L * a.KX > 3.0 * M * a.P1 ? 9.0 * a.L * a.KX : 3.0 * M * a.P1;
+  const double perA = 6.0 * M * a.P1S > 3.0 * a.L * a.KXS ? 6.0 * M * a.P1S : 3.0 * a.L * a.KXS;
+  const double perB = 9.0 * a.L * a.KXS > 3.0 * M * a.P1S ? 9.0 * a.L * a.KXS : 3.0 * M * a.P1S;
   int B = (int)(fz_scratch_budget(s) / (8.0 * (perA + perB)));
   if (B > 16) B = 16;
   if (B > nbands) B = nbands;
