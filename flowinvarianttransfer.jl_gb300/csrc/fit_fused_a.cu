@@ -72,11 +72,15 @@ __global__ void k_bench_fill(float* p, long n, unsigned seed) {
 }
 
 // shell index of live-box mode (kx, f_y, f_z) in shells of width dk (0 beyond the last shell)
-__global__ void k_bench_shells(uint16_t* seff, int K, int KX, long P1, float dk, int nsh) {
-  const long n = (long)(2 * K + 1) * P1;
+__global__ void k_bench_shells(uint16_t* seff, int K, int KX, long P1, long P1S, float dk, int nsh) {
+  const long n = (long)(2 * K + 1) * P1S;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const long col = i % P1;
-    const int kx = (int)(col % KX), fy = (int)(col / KX) - K, fz = (int)(i / P1) - K;
+    const long col = i % P1S;
+    if (col >= P1) {   // row padding
+      seff[i] = 0;
+      continue;
+    }
+    const int kx = (int)(col % KX), fy = (int)(col / KX) - K, fz = (int)(i / P1S) - K;
     const int sh = (int)(sqrtf((float)(kx * kx + fy * fy + fz * fz)) / dk) + 1;
     seff[i] = (uint16_t)(sh <= nsh ? sh : 0);
   }
@@ -111,7 +115,7 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
   const long pt = (P1 + FzTile<N>::C - 1) / FzTile<N>::C;
   const size_t in_n = pass == 0 ? (size_t)9 * units * a.KXS : pass == 1 ? (size_t)6 * N * a.P1S
                                                                          : (size_t)3 * units * N * a.P1S;
-  const size_t un = pass == 0 ? (size_t)(2 * Mtot + units * (long)N) : pass == 1 ? (size_t)KY : (size_t)6 * KY * P1;
+  const size_t un = pass == 0 ? (size_t)(2 * Mtot + units * (long)N) : pass == 1 ? (size_t)KY : (size_t)6 * KY * a.P1S;
   const size_t on = pass == 0 ? (size_t)3 * units * a.KXS : pass == 1 ? (size_t)9 * L * a.KXS : (size_t)units * 32 * pt;
   uint16_t* seff = nullptr;
   float2 *in = nullptr, *out = nullptr, *tw = nullptr;
@@ -138,13 +142,13 @@ int bench_pass(int pass, long units, int reps, double* ms, double* bytes) {
     return fz_zfwd_bin<N>(a, in, (const float2*)U, seff, (double*)out, tw, st);
   };
   if (ck(cudaMalloc(&in, in_n * 8)) && ck(cudaMalloc(&U, un * 4)) && ck(cudaMalloc(&out, on * 8)) &&
-      ck(cudaMalloc(&seff, (pass == 2 ? (size_t)KY * P1 : 1) * sizeof(uint16_t))) &&
+      ck(cudaMalloc(&seff, (pass == 2 ? (size_t)KY * a.P1S : 1) * sizeof(uint16_t))) &&
       ck(cudaMalloc(&tw, (size_t)N * 8)) && ck(cudaMalloc(&err, sizeof(int))) && ck(cudaStreamCreate(&st)) &&
       ck(cudaEventCreate(&e0)) && ck(cudaEventCreate(&e1)) && ck(cudaMemsetAsync(err, 0, sizeof(int), st)) &&
       ck(cudaMemcpyAsync(tw, h.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st))) {
     k_bench_fill<<<1216, 256, 0, st>>>((float*)in, (long)in_n * 2, 1u);
     k_bench_fill<<<1216, 256, 0, st>>>(U, (long)un, 2u);
-    if (pass == 2) k_bench_shells<<<1216, 256, 0, st>>>(seff, K, KX, P1, 14.0f * N / 512.0f, 32);
+    if (pass == 2) k_bench_shells<<<1216, 256, 0, st>>>(seff, K, KX, P1, a.P1S, 14.0f * N / 512.0f, 32);
     rc = launch();   // warm-up (kernel attributes)
     if (rc == FIT_OK && ck(cudaEventRecord(e0, st))) {
       for (int r = 0; r < reps && rc == FIT_OK; ++r) rc = launch();

@@ -930,7 +930,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
       const int f = fz_freq(e, N);
       if (col < a.P1 && f >= -a.K && f <= a.K) {
         const float2 nv = s[swzp<false>(e, mycol, C)];
-        const float2 cv = Ceff[((long)c * a.KY + f + a.K) * a.P1 + col];
+        const float2 cv = Ceff[((long)c * a.KY + f + a.K) * a.P1S + col];
         tacc[r] += cv.x * nv.x + cv.y * nv.y;
       }
     }
@@ -942,7 +942,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_BIN) k_fz_zfw
     const int e = seg * EPT + r;
     const int f = fz_freq(e, N);
     int sh = 0;
-    if (col < a.P1 && f >= -a.K && f <= a.K) sh = seff[(long)(f + a.K) * a.P1 + col];
+    if (col < a.P1 && f >= -a.K && f <= a.K) sh = seff[(long)(f + a.K) * a.P1S + col];
     if (sh != cur) {
       if (cur) atomicAdd(&bins[cur - 1], sum);
       cur = sh;

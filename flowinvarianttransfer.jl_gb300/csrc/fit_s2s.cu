@@ -229,13 +229,14 @@ int s2s_reads_kept_box(const fit_plan* p) { return fused_ok(p) && p->dealias == 
 
 
 // H (Hermitian part of the masked / embedded velocity), band shell, effective carrier and
-// binning shell for every live half-spectrum mode, compact layout [c][kz'][kx + KX ky']. CT is the
+// binning shell for every live half-spectrum mode, compact layout [c][kz'][kx + KX ky'] (the carrier
+// and binning-shell rows at stride cst: P1, or the padded P1S of the shell-to-shell batches). CT is the
 // arithmetic type: FP32 for complex64 input (H and Ceff are stored in FP32), FP64 otherwise.
 template <typename CT>
 __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, const void* F,
                                                   int f64, int inv, int two_thirds,
                                                   const uint16_t* __restrict__ shell, float2* H, float2* Ceff,
-                                                  uint16_t* seff, uint16_t* sb, int inv2, float2* Ceff2) {
+                                                  uint16_t* seff, uint16_t* sb, int inv2, float2* Ceff2, long cst) {
   typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= P1 * KY) return;
@@ -268,8 +269,8 @@ __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, in
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c)
-    Ceff[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
-  seff[(long)kz * P1 + col] = sh;
+    Ceff[((long)c * KY + kz) * cst + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
+  seff[(long)kz * cst + col] = sh;
   if (Ceff2) {   // a second invariant's carrier from the same field
 #pragma unroll
     for (int c = 0; c < 3; ++c) CA[c] = CB[c] = mkc<C2>(0, 0);
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, in
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-      Ceff2[((long)c * KY + kz) * P1 + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
+      Ceff2[((long)c * KY + kz) * cst + col] = make_float2((float)(CA[c].x + CB[c].x), (float)(CA[c].y - CB[c].y));
   }
 }
 
@@ -377,11 +378,11 @@ int fz_box_setup(fit_plan* p, const FzArgs& a, const void* F, int inv, float2* H
   if (p->io_f64)
     k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
         g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
-        seff, sb, inv2, Ceff2);
+        seff, sb, inv2, Ceff2, a.P1);
   else
     k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
         g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
-        seff, sb, inv2, Ceff2);
+        seff, sb, inv2, Ceff2, a.P1);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
@@ -441,8 +442,8 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   if (B > (int)meds.size()) B = (int)meds.size();   // no scratch for batch slots that never fill
   if (B < 1) B = 1;
   FIT_TRY(ensure(p, &s->fH, sizeof(float2) * 3 * KY * P1));
-  FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * KY * P1));
-  FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * KY * P1));
+  FIT_TRY(ensure(p, &s->fC, sizeof(float2) * 3 * KY * P1S));   // carrier and binning shell: rows of P1S
+  FIT_TRY(ensure(p, &s->fse, sizeof(uint16_t) * KY * P1S));
   FIT_TRY(ensure(p, &s->fsb, sizeof(uint16_t) * KY * P1));
   FIT_TRY(ensure(p, &s->fkd, sizeof(float) * KY));
   FIT_TRY(ensure(p, &s->fA, (size_t)(8.0 * perA * B)));
@@ -473,10 +474,12 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
   if (p->io_f64)
     k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
-        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr);
+        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr,
+        P1S);
   else
     k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
-        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr);
+        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr,
+        P1S);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   const int ntile = (int)npt;
