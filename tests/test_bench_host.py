@@ -114,6 +114,17 @@ def test_default_arguments_meet_the_contract(monkeypatch):
     assert a.warmup >= 3 and a.steps >= 1
     src = open(os.path.join(bench.ROOT, "bench.py")).read()
     import re
-    for cfg in re.findall(r'args\.config == "([a-z0-9]+)"', src):
+    for cfg in re.findall(r'args\.config == "([a-z0-9]+)"', src) + ["xpass", "ypass", "zbin"]:
         monkeypatch.setattr(sys, "argv", ["bench.py", "--config", cfg])
         assert bench.parse().config == cfg
+
+
+def test_fused_pass_hook_rejects_bad_arguments():
+    """The single-kernel benchmark hook validates its arguments before touching a GPU."""
+    import ctypes as C
+    import fit_gb300 as F
+    lib = F._lib.load()
+    ms, by = C.c_double(), C.c_double()
+    for args in ((3, 512, 1, 1), (2, 512, 9, 1), (2, 512, 0, 1), (0, 512, 17, 1), (1, 512, 513, 1),
+                 (1, 100, 1, 1), (0, 512, 16, 0)):
+        assert lib.fit_bench_fused_pass(*args, C.byref(ms), C.byref(by)) == -1, args
