@@ -716,6 +716,9 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
 #define XG_STB(q, val) xg_st<8 * (q), 0>(bB, val)
 #define XG_STC(q, val) xg_st<8 * (((q) >> 1) | (((q) & 1) << 3)), 128 * ((q) >> 1)>(cB, val)
   const int k1 = l;
+  float2 t2r[7];   // this thread's last-stage twiddles w^(jt q), q = 1..7 (the same every step)
+#pragma unroll
+  for (int q = 0; q < 7; ++q) t2r[q] = T2[GS * q + jt];
   // waits as in k_fz_xmix_reg: a first wait that runs out flags the launch and is followed by a
   // full-bound wait; a thread whose second wait runs out is broken (the lead then issues nothing
   // more) and the group carries on with whatever the buffers hold, all indices data-independent
@@ -777,7 +780,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       constexpr int q = decltype(qc)::value;
       float2 x = XG_LDA(q);
       if (q > 0) {
-        float2 w = T2[GS * (q - 1) + jt];
+        float2 w = t2r[q - 1];
         w.y = -w.y;
         x = cmul(x, w);
       }
@@ -815,7 +818,7 @@ __global__ void __launch_bounds__(XGTile<N>::NTHR, 2) k_fz_xmix_grp(FzArgs a, co
       xg_for<8>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
         float2 x = XG_LDA(q);
-        if (q > 0) x = cmul(x, T2[GS * (q - 1) + jt]);
+        if (q > 0) x = cmul(x, t2r[q - 1]);
         v[q] = x;
       });
       dftr<float2, 8, false>(v);
