@@ -173,8 +173,8 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB_Y) k_fz_yinv(
   const int ex = a.ext[b][0], ey = a.ext[b][1];
   if (k0 > ex) return;   // no mode of the mediator's shell at these kx (outputs never read)
   const long ib = ((((long)b * 3 + c) * 2 + v) * N + z) * a.P1S;
+  // the twiddle table is first read after the transform's first stage, behind its block barrier
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
   const long obase = ((((long)b * 3 + c) * 3 + j) * N + z) * N;
   ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
@@ -869,8 +869,8 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_yfwd(Fz
   const int z = blockIdx.z / nkt, k0 = (blockIdx.z % nkt) * C;
   const int c = blockIdx.y, b = blockIdx.x;
   const long ib = ((long)b * 3 + c) * a.L + (long)N * z;
+  // the twiddle table is first read after the transform's first stage, behind its block barrier
   for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
   const long obase = (((long)b * 3 + c) * N + z) * a.P1S;
   ct_fft_mapped<float2, false, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
