@@ -991,8 +991,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv_bo
   const int tid = threadIdx.x;
   const long c0 = (long)blockIdx.z * C;
   const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
-  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];   // read after the transform's first barrier
   const float2* Hc = H + ((long)a.hidx[b] * 3 + c) * a.KY * a.P1;
   float2* ob = out + (((long)b * 3 + c) * 2 + v) * N * a.P1S;
   ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
@@ -1033,8 +1032,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zfwd_st
   const int tid = threadIdx.x;
   const long c0 = (long)blockIdx.z * C;
   const int c = blockIdx.y, b = blockIdx.x;
-  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];   // read after the transform's first barrier
   const float2* ib = in + ((long)b * 3 + c) * N * a.P1S;
   float2* ob = out + ((long)b * 3 + c) * a.KY * a.P1;
   ct_fft_mapped<float2, false, N, C, NT, TT::EPT, false, PM>(
@@ -1067,8 +1065,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uz(FzAr
   const int tid = threadIdx.x;
   const long c0 = (long)blockIdx.y * C;
   const int c = blockIdx.x;
-  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];   // read after the transform's first barrier
   const float2* Hc = H + (long)c * a.KY * a.P1;
   float2* oc = out + (long)c * N * a.P1;
   ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
@@ -1097,8 +1094,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_uy(FzAr
   const int tid = threadIdx.x;
   const int nkt = (a.KX + C - 1) / C;
   const int z = blockIdx.y / nkt, k0 = (blockIdx.y % nkt) * C, c = blockIdx.x;
-  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];   // read after the transform's first barrier
   const float2* ib = in + ((long)c * N + z) * a.P1;
   float2* ob = out + ((long)c * N + z) * N * a.KX;
   ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
@@ -1126,8 +1122,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_ux(FzAr
   float2* tw = s + E;
   const int tid = threadIdx.x;
   const long l0 = (long)blockIdx.x * 2 * C;   // lines of all three components, 2C per block
-  for (int t = tid; t < N; t += NT) tw[t] = twg[t];
-  __syncthreads();
+  for (int t = tid; t < N; t += NT) tw[t] = twg[t];   // read after the transform's first barrier
   ct_fft_mapped<float2, true, N, C, NT, TT::EPT, false, PM>(
       s, tw, tid,
       [&](int, int, int k, int col) -> float2 {
