@@ -18,6 +18,7 @@ from .types import (BandToBandResult, DivergentDecomposition, DirectSumBackend, 
                     KineticEnergy, ModeToModeTransferMethod, ModeToModeTriadResult, NoDecomposition,
                     OrszagTwoThirds, PaddedThreeHalves, PartialFluxResult, PassiveScalar, RotationalDecomposition,
                     ShellToShellResult, ShellToShellTransferMethod, SpectralFluxMethod, SpectralFluxResult,
+                    CoarseGrainingFluxMethod,
                     ToroidalPoloidalDecomposition)
 
 
@@ -326,12 +327,19 @@ def calculate_scalar_mode_to_mode_transfer(velocity_hat, scalar_hat, ks, **kw):
 
 
 # ---- unified dispatch ----------------------------------------------------------------------------
-def calculate_energy_transfer(method, velocity_hat, ks, **kw):
-    """``calculate_energy_transfer`` (``src/FlowInvariantTransfer.jl:248-293``) for the spectral methods."""
+def calculate_energy_transfer(method, velocity_data, coords_or_ks, **kw):
+    """``calculate_energy_transfer`` (``src/FlowInvariantTransfer.jl:248-293``): spectral flux,
+    shell-to-shell and mode-to-mode take a spectral field and ``ks``; coarse-graining takes a tuple
+    of real fields and a tuple of coordinate vectors."""
     if isinstance(method, SpectralFluxMethod):
-        return calculate_spectral_flux(velocity_hat, ks, binning=method.binning, **kw)
+        return calculate_spectral_flux(velocity_data, coords_or_ks, binning=method.binning, **kw)
     if isinstance(method, ShellToShellTransferMethod):
-        return calculate_shell_to_shell_transfer(velocity_hat, ks, binning=method.binning, **kw)
+        return calculate_shell_to_shell_transfer(velocity_data, coords_or_ks, binning=method.binning, **kw)
     if isinstance(method, ModeToModeTransferMethod):
-        return calculate_mode_to_mode_transfer(velocity_hat, ks, **kw)
+        if method.invariant is not None:
+            kw.setdefault("invariant", method.invariant)
+        return calculate_mode_to_mode_transfer(velocity_data, coords_or_ks, **kw)
+    if isinstance(method, CoarseGrainingFluxMethod):
+        from .closure import calculate_coarse_graining_flux
+        return calculate_coarse_graining_flux(velocity_data, coords_or_ks, method.scale, method.filter, **kw)
     raise ValueError(f"unsupported method {method!r}")

@@ -211,7 +211,17 @@ class ShellToShellTransferMethod:
 
 @dataclass(frozen=True)
 class ModeToModeTransferMethod:
-    pass
+    """``ModeToModeTransferMethod(; binning=nothing, invariant=KineticEnergy())`` (``src/Types.jl:288-295``)."""
+    binning: Any = None
+    invariant: Any = None
+
+
+@dataclass(frozen=True)
+class CoarseGrainingFluxMethod:
+    """``CoarseGrainingFluxMethod(filter, scale)`` (``src/Types.jl:241-244``): the filter kernel and
+    its length scale ell."""
+    filter: Any
+    scale: float
 
 
 # ---- results ------------------------------------------------------------------------------------
