@@ -246,3 +246,16 @@ def test_toroidal_poloidal_decomposition():    # runtests.jl:634-659
     _, Tw, _ = O.spectral_flux(u16, ks16, ("linear", 1.0), "two_thirds")
     assert np.max(np.abs(Tw)) > 1e-6
     assert np.max(np.abs(T - Tw)) <= 1e-12 * np.max(np.abs(Tw))
+
+
+def test_filter_responses():                   # runtests.jl:101-127
+    ell = 1.0
+    assert O.filter_response("sharp", 2.0, ell) == 1.0          # passes k < pi / ell
+    assert O.filter_response("sharp", 4.0, ell) == 0.0
+    g1, g2 = O.filter_response("gaussian", 2.0, ell), O.filter_response("gaussian", 4.0, ell)
+    assert 0.0 < g2 < g1 <= 1.0                                 # in (0, 1], decaying with k
+    assert O.filter_response("tophat", 0.0, ell) == pytest.approx(1.0)
+    # applied in spectral space: k = 0..3 < pi pass, k = 4 is removed
+    k_mag = np.array([0.0, 1.0, 2.0, 3.0, 4.0])
+    u_out = O.filter_response("sharp", k_mag, 1.0) * np.ones(5, complex)
+    assert np.allclose(u_out, [1, 1, 1, 1, 0])
