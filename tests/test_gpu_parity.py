@@ -341,3 +341,27 @@ def test_fused_shell_to_shell_two_batches(inv):
                                                 spectral=F.GB300Spectral(32), execution=F.GB300Execution("batched"))
         assert rel(r.transfer_matrix, T) < 1e-5
         assert rel(r.net_transfer, net) < 1e-4
+
+
+@pytest.mark.parametrize("seed", [3, 11])
+def test_fused_shell_to_shell_conservation_floor(seed):
+    """Energy conservation of the raw FP32 pipeline on an exactly solenoidal FP64 input (FP64 host
+    buffers, FP32 arithmetic): sum_nm T(n,m) vanishes in exact arithmetic for a divergence-free,
+    dealiased field, so |sum T| / sum |T| measures the pipeline's own rounding. The FP32 figure
+    stays at the single-precision floor (measured 3.1e-8 and 3.6e-8 on GB300 for these two fields) and
+    the FP64 path on the same field at the double-precision floor (below 1e-16)."""
+    F.clear_plans()
+    u, ks = spectrum_field((64, 64, 64), e_config2, seed=seed)
+    assert u.dtype == np.complex128
+    b = F.LinearBinning(2.0)
+    res = {}
+    for prec, ex in ((32, "batched"), (64, "plain")):
+        r = F.calculate_shell_to_shell_transfer(u, ks, binning=b, spectral=F.GB300Spectral(prec),
+                                                execution=F.GB300Execution(ex))
+        T = np.asarray(r.transfer_matrix, dtype=np.float64)
+        res[prec] = (T, abs(T.sum()) / np.abs(T).sum())
+    print(f"seed {seed}: conservation FP32 {res[32][1]:.3e}, FP64 {res[64][1]:.3e}, "
+          f"FP32 vs FP64 {rel(res[32][0], res[64][0]):.3e}")
+    assert res[64][1] < 1e-12
+    assert res[32][1] < 3e-7
+    assert rel(res[32][0], res[64][0]) < 1e-5
