@@ -224,7 +224,10 @@ static int stage_in(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int
 // copy engines on a coherent host link); other host memory goes through 8 pitched 3D copies per
 // component (one per octant of the box). Modes outside the box are left unwritten in the staging
 // buffer and are never read. FIT_KEPT_BOX_COPY_ENGINE=1 selects the 3D copies for pinned memory too.
-static int stage_in_kept_box(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int ncomp, const void** out) {
+// With `defer`, a pinned field is not read here: the shell-to-shell step reads it into the staging
+// buffer itself (p->kept_src), overlapping the read with its first passes.
+static int stage_in_kept_box(fit_plan* p, fit_dbuf* b, const void* src, size_t bytes, int ncomp, const void** out,
+                             bool defer = false) {
   if (src == nullptr) {
     *out = nullptr;
     return FIT_OK;
@@ -237,7 +240,8 @@ static int stage_in_kept_box(fit_plan* p, fit_dbuf* b, const void* src, size_t b
   const bool dma = env && env[0] == '1';
   if (!dma && cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost &&
       at.devicePointer != nullptr && ((uintptr_t)at.devicePointer % eb) == 0) {
-    FIT_TRY(copy_kept_box(at.devicePointer, b->p, g.N, ncomp, (int)eb, p->stream));
+    if (defer) p->kept_src = at.devicePointer;
+    else FIT_TRY(copy_kept_box(at.devicePointer, b->p, g.N, ncomp, (int)eb, p->stream));
     long kept = 1;
     for (int d = 0; d < 3; ++d) kept *= 2L * (g.N[d] / 3 - 1) + 1;
     p->h2d_total += (size_t)kept * ncomp * eb;
@@ -607,8 +611,9 @@ static int s2s_stage(fit_plan* p, const void* u_hat, const void* adv_hat, int in
   FIT_TRY(check_invariant(p, invariant, p->M));
   API_CHECK(mode == FIT_S2S_PLAIN || mode == FIT_S2S_BATCHED, FIT_ERR_ARG, "unknown shell-to-shell mode %d", mode);
   const size_t fb = cbytes(p) * p->g.Ntot * p->M, ab = cbytes(p) * p->g.Ntot * p->Dadv;
+  p->kept_src = nullptr;
   if (mode == FIT_S2S_BATCHED && ptr_kind != FIT_PTR_DEVICE && s2s_reads_kept_box(p)) {
-    FIT_TRY(stage_in_kept_box(p, &p->in_u, u_hat, fb, p->M, ud));
+    FIT_TRY(stage_in_kept_box(p, &p->in_u, u_hat, fb, p->M, ud, true));
     FIT_TRY(stage_in_kept_box(p, &p->in_a, adv_hat, ab, p->Dadv, ad));
   } else {
     FIT_TRY(stage_in(p, &p->in_u, u_hat, fb, ptr_kind, ud));
@@ -629,7 +634,9 @@ static int s2s_run(fit_plan* p, const void* ud, const void* ad, int invariant, i
   double* Td = (double*)p->outd.p;
   FIT_CUDA_CHECK(cudaMemsetAsync(Td, 0, sizeof(double) * (size_t)nsh * nsh, p->stream));
   if (mode == FIT_S2S_BATCHED) {
-    FIT_TRY(s2s_batched(p, ud, ad, invariant, Td));
+    const int rc = s2s_batched(p, ud, ad, invariant, Td);
+    p->kept_src = nullptr;   // read (or abandoned) by this call
+    FIT_TRY(rc);
     FIT_TRY(s2s_check(p));
   } else if (p->prec == 64) {
     FIT_TRY(carrier_and_bin_setup<double>(p, ud, invariant));

@@ -21,6 +21,18 @@ int fz_dispatch_a(int N, const FzArgs& a, const float2* H, const float2* Ceff, c
   }
 }
 
+// zinv of a batch over pencil tiles [t0, t1) (1 when N is not built here).
+int fz_zinv_a(int N, const FzArgs& a, const float2* H, const float* kd, float2* bufA, const float2* tw, int t0,
+               int t1, cudaStream_t st) {
+  switch (N) {
+    case 64: return fz_zinv_tiles<64>(a, H, kd, bufA, tw, t0, t1, st);
+    case 128: return fz_zinv_tiles<128>(a, H, kd, bufA, tw, t0, t1, st);
+    case 256: return fz_zinv_tiles<256>(a, H, kd, bufA, tw, t0, t1, st);
+    case 512: return fz_zinv_tiles<512>(a, H, kd, bufA, tw, t0, t1, st);
+    default: return 1;
+  }
+}
+
 // Pencils per tile of the fused strided passes for transform length N (0 when not built here).
 int fz_tile_cols_a(int N) {
   switch (N) {

@@ -16,6 +16,18 @@ int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, c
   }
 }
 
+// zinv of a batch over pencil tiles [t0, t1) (1 when N is not built here).
+int fz_zinv_b(int N, const FzArgs& a, const float2* H, const float* kd, float2* bufA, const float2* tw, int t0,
+               int t1, cudaStream_t st) {
+  switch (N) {
+    case 96: return fz_zinv_tiles<96>(a, H, kd, bufA, tw, t0, t1, st);
+    case 192: return fz_zinv_tiles<192>(a, H, kd, bufA, tw, t0, t1, st);
+    case 384: return fz_zinv_tiles<384>(a, H, kd, bufA, tw, t0, t1, st);
+    case 768: return fz_zinv_tiles<768>(a, H, kd, bufA, tw, t0, t1, st);
+    default: return 1;
+  }
+}
+
 // Pencils per tile of the fused strided passes for transform length N (0 when not built here).
 int fz_tile_cols_b(int N) {
   switch (N) {

@@ -65,6 +65,8 @@ struct FzArgs {
   const float* wbox;
   int widx[16];
   long long wlim;   // first bound of the x pass's copy waits (fit_wait_cycles)
+  int tz0;          // zinv: first pencil tile of the launch (launches over a range of tiles)
+  int nozinv;       // fz_batch: the batch's zinv outputs are already written (tile-range launches)
 };
 
 // the padded row strides of a batch's intermediates, from its KX and P1
@@ -106,7 +108,7 @@ __global__ void __launch_bounds__(FzTile<N>::NTHR, FzTile<N>::MINB) k_fz_zinv(Fz
   float2* s = reinterpret_cast<float2*>(fit_smem_raw);
   float2* tw = s + E;
   const int tid = threadIdx.x;
-  const int tile = blockIdx.z;
+  const int tile = blockIdx.z + a.tz0;
   const long c0 = (long)tile * C;
   const int c = blockIdx.y >> 1, v = blockIdx.y & 1, b = blockIdx.x;
   const int m = a.med[b];
@@ -1303,6 +1305,30 @@ int fz_terms(const FzArgs& a, const float2* H, const float* kd, const float* U, 
   return FIT_OK;
 }
 
+// ---- zinv of a batch over pencil tiles [t0, t1) (the rest of the batch then runs with nozinv) ----
+template <int N>
+int fz_zinv_tiles(const FzArgs& a, const float2* H, const float* kd, float2* bufA, const float2* tw, int t0, int t1,
+                  cudaStream_t st) {
+  typedef FzTile<N> TT;
+  const size_t sm = TT::SMEM;
+  FIT_TRY(ct_prep_fused(k_fz_zinv<N>, sm, TT::NTHR));
+  if (t1 <= t0) return FIT_OK;
+  const int pt = (int)((a.P1 + TT::C - 1) / TT::C);
+  double zin_b = 0.0;   // the tile range's share of the batch's algorithmic bytes (as in fz_batch)
+  for (int b = 0; b < a.nb; ++b) {
+    const double ex = a.ext[b][0], ey = a.ext[b][1], ez = a.ext[b][2];
+    const double Pm = (ex + 1.0) * (2.0 * ey + 1.0);
+    zin_b += 8.0 * 6.0 * N * Pm + 2.0 * (2.0 * ez + 1.0) * Pm;
+  }
+  FzArgs ar = a;
+  ar.tz0 = t0;
+  fit_prof_begin(PK_S2S_ZINV, zin_b * (t1 - t0) / pt, st);
+  k_fz_zinv<N><<<dim3(a.nb, 6, t1 - t0), TT::NTHR, sm, st>>>(ar, H, kd, bufA, tw);
+  fit_prof_end(st);
+  FIT_LAUNCH_CHECK();
+  return FIT_OK;
+}
+
 // ---- host launcher for one batch (instantiated per transform length) -------------------------
 template <int N>
 int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
@@ -1329,10 +1355,12 @@ int fz_batch(const FzArgs& a, const float2* H, const float2* Ceff, const uint16_
     zin_b += cpx * 6.0 * N * Pm + 2.0 * (2.0 * ez + 1.0) * Pm;
     yin_b += cpx * (6.0 * N * Pm + 9.0 * (double)N * N * (ex + 1.0));
   }
-  fit_prof_begin(PK_S2S_ZINV, zin_b, st);
-  k_fz_zinv<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, kd, bufA, tw);
-  fit_prof_end(st);
-  FIT_LAUNCH_CHECK();
+  if (!a.nozinv) {
+    fit_prof_begin(PK_S2S_ZINV, zin_b, st);
+    k_fz_zinv<N><<<dim3(a.nb, 6, pt), TT::NTHR, sm, st>>>(a, H, kd, bufA, tw);
+    fit_prof_end(st);
+    FIT_LAUNCH_CHECK();
+  }
   fit_prof_begin(PK_S2S_YINV, yin_b, st);
   FIT_TRY(fz_yinv<N>(a, bufA, kd, bufB, tw, err, N, st));
   fit_prof_end(st);

@@ -464,73 +464,127 @@ int shell_table_i64(const GridDesc& g, const uint16_t* sh, int64_t* out, cudaStr
   return FIT_OK;
 }
 
-// One block per kept row (component, z, y): the row's two x runs [0, K0] and [N0 - K0, N0).
+// Rows (component c, z, y) of the kept box whose |signed y frequency| lies in [ya, yb), numbered
+// (c, iz, j): j runs over the range's non-negative y values first, then its negative ones.
+struct KeptRows {
+  int N0, N1, N2, K0, K1, K2;
+  int ya, yb;
+  int npos, nyc;   // non-negative y values of the range, and all of them
+  long nrows;
+};
+
+// element offset of row r's x = 0 in the column-major field
+FIT_D long kept_row_base(const KeptRows& k, long r) {
+  const int j = (int)(r % k.nyc);
+  const long q = r / k.nyc;
+  const int nz = 2 * k.K2 + 1;
+  const int iz = (int)(q % nz), c = (int)(q / nz);
+  const int y = j < k.npos ? k.ya + j : k.N1 - (k.yb - 1) + (j - k.npos);
+  const int z = iz <= k.K2 ? iz : k.N2 - nz + iz;
+  return (((long)c * k.N2 + z) * k.N1 + y) * (long)k.N0;
+}
+
+// The rows' kept elements (x in [0, K0] and [N0 - K0, N0)), flat over rows x elements so that a
+// warp reads consecutive elements of a row; every thread has four loads in flight before its
+// stores, so a small grid still keeps enough reads outstanding on the host link.
 template <typename E>
-__global__ void __launch_bounds__(128) k_copy_kept_box(const E* __restrict__ src, E* __restrict__ dst, int N0,
-                                                       int N1, int N2, int K0, int K1, int K2) {
-  const int ny = 2 * K1 + 1, nz = 2 * K2 + 1, nx = 2 * K0 + 1;
-  const long r = blockIdx.x;
-  const int iy = (int)(r % ny), iz = (int)((r / ny) % nz), c = (int)(r / ((long)ny * nz));
-  const int y = iy <= K1 ? iy : N1 - ny + iy, z = iz <= K2 ? iz : N2 - nz + iz;
-  const long base = (((long)c * N2 + z) * N1 + y) * (long)N0;
-  for (int ix = threadIdx.x; ix < nx; ix += blockDim.x) {
-    const int x = ix <= K0 ? ix : N0 - nx + ix;
-    dst[base + x] = src[base + x];
+__global__ void __launch_bounds__(256) k_copy_kept_rows(const E* __restrict__ src, E* __restrict__ dst, KeptRows k) {
+  const int nx = 2 * k.K0 + 1;
+  const long n = k.nrows * nx, stride = (long)gridDim.x * blockDim.x;
+  for (long i0 = blockIdx.x * (long)blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    E v[4];
+    long at[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const long i = i0 + u * stride;
+      at[u] = -1;
+      if (i < n) {
+        const long r = i / nx;
+        const int ix = (int)(i - r * nx);
+        at[u] = kept_row_base(k, r) + (ix <= k.K0 ? ix : k.N0 - nx + ix);
+        v[u] = src[at[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (at[u] >= 0) dst[at[u]] = v[u];
   }
 }
 
 // The same copy of 8-byte elements (complex64) in 16-byte pairs, for an even row length and 16-byte
-// aligned arrays (so every row starts on a 16-byte boundary): run A, x in [0, K0], from x = 0 with a
-// single element at its end when its length is odd; run B, x in [N0 - K0, N0), with a single
-// element at its start when N0 - K0 is odd. Each thread issues its first two pairs' loads before
-// any store, so a block keeps up to 256 loads of 16 bytes in flight over the host link.
-__global__ void __launch_bounds__(128) k_copy_kept_box_c64(const uint2* __restrict__ src, uint2* __restrict__ dst,
-                                                           int N0, int N1, int N2, int K0, int K1, int K2) {
-  const int ny = 2 * K1 + 1, nz = 2 * K2 + 1;
-  const long r = blockIdx.x;
-  const int iy = (int)(r % ny), iz = (int)((r / ny) % nz), c = (int)(r / ((long)ny * nz));
-  const int y = iy <= K1 ? iy : N1 - ny + iy, z = iz <= K2 ? iz : N2 - nz + iz;
-  const long base = (((long)c * N2 + z) * N1 + y) * (long)N0;   // even: N0 is even
-  const int pA = (K0 + 1) >> 1;
-  const int sB = N0 - K0, hB = sB & 1;
-  const int pB = (N0 - sB - hB) >> 1;
-  const int np = pA + pB, qB = (sB + hB) >> 1;   // pair index of run B's first pair
-  const uint4* s4 = reinterpret_cast<const uint4*>(src + base);
-  uint4* d4 = reinterpret_cast<uint4*>(dst + base);
-  uint4 v[2];
-  int at[2];
+// aligned arrays (every row starts on a 16-byte boundary): run A, x in [0, K0], in pairs from x = 0;
+// run B, x in [N0 - K0, N0), in pairs ending at N0; the single elements left at odd run ends (x = K0
+// when K0 + 1 is odd, x = N0 - K0 when that is odd) in a second loop.
+__global__ void __launch_bounds__(256) k_copy_kept_rows_c64(const uint2* __restrict__ src, uint2* __restrict__ dst,
+                                                            KeptRows k) {
+  const int pA = (k.K0 + 1) >> 1, sB = k.N0 - k.K0, hB = sB & 1;
+  const int pB = (k.N0 - sB - hB) >> 1, np = pA + pB, qB = (sB + hB) >> 1;   // qB: run B's first pair
+  const long n = k.nrows * np, stride = (long)gridDim.x * blockDim.x;
+  const long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const uint4* s4 = reinterpret_cast<const uint4*>(src);
+  uint4* d4 = reinterpret_cast<uint4*>(dst);
+  for (long i0 = t0; i0 < n; i0 += 4 * stride) {
+    uint4 v[4];
+    long at[4];
 #pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    const int t = threadIdx.x + 128 * k;
-    at[k] = t < pA ? t : (t < np ? qB + (t - pA) : -1);
-    if (at[k] >= 0) v[k] = s4[at[k]];
+    for (int u = 0; u < 4; ++u) {
+      const long i = i0 + u * stride;
+      at[u] = -1;
+      if (i < n) {
+        const long r = i / np;
+        const int t = (int)(i - r * np);
+        at[u] = (kept_row_base(k, r) >> 1) + (t < pA ? t : qB + (t - pA));
+        v[u] = s4[at[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (at[u] >= 0) d4[at[u]] = v[u];
   }
-  uint2 e0 = make_uint2(0u, 0u);
-  if (threadIdx.x == 0 && ((K0 + 1) & 1)) e0 = src[base + K0];
-  if (threadIdx.x == 1 && hB) e0 = src[base + sB];
-#pragma unroll
-  for (int k = 0; k < 2; ++k)
-    if (at[k] >= 0) d4[at[k]] = v[k];
-  if (threadIdx.x == 0 && ((K0 + 1) & 1)) dst[base + K0] = e0;
-  if (threadIdx.x == 1 && hB) dst[base + sB] = e0;
-  for (int t = threadIdx.x + 256; t < np; t += 128) {   // rows longer than 512 pairs of kept elements
-    const int q = t < pA ? t : qB + (t - pA);
-    d4[q] = s4[q];
+  const int s0 = (k.K0 + 1) & 1, ns = s0 + hB;
+  for (long i = t0; i < k.nrows * ns; i += stride) {
+    const long r = i / ns;
+    const int w = (int)(i - r * ns);
+    const long e = kept_row_base(k, r) + ((s0 && w == 0) ? k.K0 : sB);
+    dst[e] = src[e];
   }
 }
 
-int copy_kept_box(const void* src, void* dst, const int* N, int ncomp, int eb, cudaStream_t st) {
-  const int K0 = N[0] / 3 - 1, K1 = N[1] / 3 - 1, K2 = N[2] / 3 - 1;
-  const long rows = (long)ncomp * (2 * K1 + 1) * (2 * K2 + 1);
-  if (rows <= 0 || K0 < 0) return FIT_OK;
-  if (eb == 8 && N[0] % 2 == 0 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0)
-    k_copy_kept_box_c64<<<(unsigned)rows, 128, 0, st>>>((const uint2*)src, (uint2*)dst, N[0], N[1], N[2], K0, K1, K2);
+int copy_kept_rows(const void* src, void* dst, const int* N, int ncomp, int eb, int ya, int yb, int max_blocks,
+                   cudaStream_t st) {
+  KeptRows k;
+  k.N0 = N[0];
+  k.N1 = N[1];
+  k.N2 = N[2];
+  k.K0 = N[0] / 3 - 1;
+  k.K1 = N[1] / 3 - 1;
+  k.K2 = N[2] / 3 - 1;
+  if (yb > k.K1 + 1) yb = k.K1 + 1;
+  if (ya < 0) ya = 0;
+  k.ya = ya;
+  k.yb = yb;
+  k.npos = yb - ya;
+  k.nyc = k.npos + (yb - (ya > 1 ? ya : 1));
+  k.nrows = (long)ncomp * (2 * k.K2 + 1) * k.nyc;
+  if (k.K0 < 0 || k.npos <= 0 || k.nrows <= 0) return FIT_OK;
+  const bool pairs = eb == 8 && N[0] % 2 == 0 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0;
+  const long items = k.nrows * (pairs ? (long)k.K0 + 1 : 2L * k.K0 + 1);   // pairs: about (2 K0 + 1) / 2 a row
+  long blocks = (items + 4 * 256 - 1) / (4 * 256);
+  if (blocks > 152L * 64) blocks = 152L * 64;
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
+  const unsigned nb = (unsigned)blocks;
+  if (pairs)
+    k_copy_kept_rows_c64<<<nb, 256, 0, st>>>((const uint2*)src, (uint2*)dst, k);
   else if (eb == 16)
-    k_copy_kept_box<uint4><<<(unsigned)rows, 128, 0, st>>>((const uint4*)src, (uint4*)dst, N[0], N[1], N[2], K0, K1, K2);
+    k_copy_kept_rows<uint4><<<nb, 256, 0, st>>>((const uint4*)src, (uint4*)dst, k);
   else
-    k_copy_kept_box<uint2><<<(unsigned)rows, 128, 0, st>>>((const uint2*)src, (uint2*)dst, N[0], N[1], N[2], K0, K1, K2);
+    k_copy_kept_rows<uint2><<<nb, 256, 0, st>>>((const uint2*)src, (uint2*)dst, k);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
+}
+
+int copy_kept_box(const void* src, void* dst, const int* N, int ncomp, int eb, cudaStream_t st) {
+  return copy_kept_rows(src, dst, N, ncomp, eb, 0, N[1] / 3, 0, st);
 }
 
 __global__ void k_sh_from_i64(const int64_t* __restrict__ idx, long n, int nsh, uint16_t* __restrict__ out,

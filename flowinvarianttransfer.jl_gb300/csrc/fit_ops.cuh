@@ -142,8 +142,12 @@ int bin_density(const GridDesc& g, const typename Vec2<T>::t* nh, long nh_batch_
 // Copies the box of modes every axis keeps under the 2/3 rule (indices [0, K_d] and [N_d - K_d, N_d),
 // K_d = N_d/3 - 1) of ncomp column-major 3D fields from src to the same positions of dst; elements of
 // eb = 8 or 16 bytes. src may be host memory the device can address (pinned, mapped): the device
-// then reads it over the host link itself, one block per kept row.
+// then reads it over the host link itself.
 int copy_kept_box(const void* src, void* dst, const int* N, int ncomp, int eb, cudaStream_t st);
+// The same copy restricted to the kept rows whose |signed y frequency| lies in [ya, yb), on at most
+// max_blocks blocks of 256 threads (0: no limit).
+int copy_kept_rows(const void* src, void* dst, const int* N, int ncomp, int eb, int ya, int yb, int max_blocks,
+                   cudaStream_t st);
 
 // Half spectrum on the transform grid -> full N-grid array (user layout), 2/3 mask applied.
 template <typename T>

@@ -47,6 +47,9 @@ struct fit_plan {
   long shell_gen = 0;    // bumped whenever the shell table changes: graphs and mode lists key on it
   // batched shell-to-shell state (fit_s2s.cu)
   void* s2s = nullptr;
+  // device address of a pinned host field that the batched shell-to-shell call reads into its
+  // staging buffer itself (set when the call's inputs are staged, nullptr otherwise)
+  const void* kept_src = nullptr;
   // batched partial-flux state (fit_partial.cu)
   void* partial_state = nullptr;
   // smooth-band weights on the transform grid's half spectrum (fit_band.cu)

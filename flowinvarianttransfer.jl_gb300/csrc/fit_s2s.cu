@@ -30,6 +30,10 @@ int fz_tile_cols_b(int N);
 int fz_dispatch_b(int N, const FzArgs& a, const float2* H, const float2* Ceff, const uint16_t* seff,
                   const float* kd, const float* U, float2* bufA, float2* bufB, double* partial,
                   const float2* tw, int* err, cudaStream_t st);
+int fz_zinv_a(int N, const FzArgs& a, const float2* H, const float* kd, float2* bufA, const float2* tw, int t0,
+              int t1, cudaStream_t st);
+int fz_zinv_b(int N, const FzArgs& a, const float2* H, const float* kd, float2* bufA, const float2* tw, int t0,
+              int t1, cudaStream_t st);
 
 struct S2SState {
   cudaGraphExec_t exec = nullptr;
@@ -57,7 +61,15 @@ struct S2SState {
   int zl_nsh = -1;
   long zl_sgen = -1;
   long key_sgen = -1;
+  const void* key_h = nullptr;   // the pinned host field a captured graph reads (nullptr: none)
   double budget = 0.0;   // batch scratch budget in bytes, fixed at the plan's first fused call
+  // read of a pinned host field over the host link in chunks of y rows on a second stream (on a
+  // small grid, leaving most SMs to the compute it overlaps), each chunk joined to the set-up and
+  // first z pass that need only its rows
+  cudaStream_t cs = nullptr;
+  cudaEvent_t cfork = nullptr;
+  std::vector<cudaEvent_t> cev;
+  int cblocks = 0;
 };
 
 // Scratch for a batch of mediators (zinv and yinv outputs, the largest intermediates): 80 GB when
@@ -81,6 +93,9 @@ void s2s_free(fit_plan* p) {
   S2SState* s = (S2SState*)p->s2s;
   if (!s) return;
   if (s->exec) cudaGraphExecDestroy(s->exec);
+  for (cudaEvent_t e : s->cev) cudaEventDestroy(e);
+  if (s->cfork) cudaEventDestroy(s->cfork);
+  if (s->cs) cudaStreamDestroy(s->cs);
   fit_dbuf* bufs[] = {&s->occ_dev, &s->fH, &s->fC, &s->fse,  &s->fsb,  &s->fkd,  &s->fA,
                       &s->fB,      &s->fpart, &s->ferr, &s->zoff, &s->zent, &s->zfill, &s->fN};
   for (fit_dbuf* b : bufs)
@@ -236,12 +251,13 @@ template <typename CT>
 __global__ void __launch_bounds__(256) k_fz_setup(GridDesc g, KTab kt, int K, int KX, int KY, long P1, const void* F,
                                                   int f64, int inv, int two_thirds,
                                                   const uint16_t* __restrict__ shell, float2* H, float2* Ceff,
-                                                  uint16_t* seff, uint16_t* sb, int inv2, float2* Ceff2, long cst) {
+                                                  uint16_t* seff, uint16_t* sb, int inv2, float2* Ceff2, long cst,
+                                                  long col0, long ncol) {
   typedef typename Vec2<CT>::t C2;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= P1 * KY) return;
-  const long col = i % P1;
-  const int kz = (int)(i / P1);
+  if (i >= ncol * KY) return;
+  const long col = col0 + i % ncol;   // pencils [col0, col0 + ncol) of every kz'
+  const int kz = (int)(i / ncol);
   const int kx = (int)(col % KX), ky = (int)(col / KX);
   KIdx kA, kB;
   map_pair(g, kx, fmod_pos(ky - K, g.M[1]), fmod_pos(kz - K, g.M[2]), &kA, &kB);
@@ -378,11 +394,11 @@ int fz_box_setup(fit_plan* p, const FzArgs& a, const void* F, int inv, float2* H
   if (p->io_f64)
     k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
         g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
-        seff, sb, inv2, Ceff2, a.P1);
+        seff, sb, inv2, Ceff2, a.P1, 0L, a.P1);
   else
     k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
         g, p->kt, a.K, a.KX, a.KY, a.P1, F, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ceff,
-        seff, sb, inv2, Ceff2, a.P1);
+        seff, sb, inv2, Ceff2, a.P1, 0L, a.P1);
   fit_prof_end(p->stream);
   FIT_LAUNCH_CHECK();
   return FIT_OK;
@@ -471,40 +487,32 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   uint16_t* se = (uint16_t*)s->fse.p;
   uint16_t* sbp = (uint16_t*)s->fsb.p;
   const long nset = P1 * KY;
-  fit_prof_begin(PK_CARRIER, (double)nset * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
-  if (p->io_f64)
-    k_fz_setup<double><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
-        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr,
-        P1S);
-  else
-    k_fz_setup<float><<<(unsigned)((nset + 255) / 256), 256, 0, p->stream>>>(
-        g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se, sbp, -1, nullptr,
-        P1S);
-  fit_prof_end(p->stream);
-  FIT_LAUNCH_CHECK();
   const int ntile = (int)npt;
-  if (s->zl_edges != p->cached_edges || s->zl_dims != p->cached_dims || s->zl_f32 != p->cached_f32 ||
-      s->zl_nsh != nsh || s->zl_sgen != p->shell_gen) {   // shell table changed: rebuild the z-pass mode lists (an eager call)
-    const long nmodes = nset, nl = (long)nsh * ntile;
-    FIT_TRY(ensure(p, &s->zoff, sizeof(unsigned) * (size_t)(nl + 1)));
-    FIT_TRY(ensure(p, &s->zfill, sizeof(unsigned) * (size_t)nl));
-    FIT_TRY(ensure(p, &s->zent, sizeof(uint16_t) * (size_t)nmodes));
-    FIT_CUDA_CHECK(cudaMemsetAsync(s->zfill.p, 0, sizeof(unsigned) * (size_t)nl, p->stream));
-    const unsigned gb = (unsigned)((nmodes + 255) / 256);
-    k_zl_count<<<gb, 256, 0, p->stream>>>(sbp, nmodes, P1, C, ntile, (unsigned*)s->zfill.p);
-    FIT_LAUNCH_CHECK();
-    k_zl_scan<<<1, 1024, 0, p->stream>>>((const unsigned*)s->zfill.p, nl, (unsigned*)s->zoff.p);
-    FIT_LAUNCH_CHECK();
-    FIT_CUDA_CHECK(cudaMemsetAsync(s->zfill.p, 0, sizeof(unsigned) * (size_t)nl, p->stream));
-    k_zl_fill<<<gb, 256, 0, p->stream>>>(sbp, nmodes, P1, C, ntile, (const unsigned*)s->zoff.p, (unsigned*)s->zfill.p,
-                                         (uint16_t*)s->zent.p);
-    FIT_LAUNCH_CHECK();
-    s->zl_edges = p->cached_edges;
-    s->zl_dims = p->cached_dims;
-    s->zl_f32 = p->cached_f32;
-    s->zl_nsh = nsh;
-    s->zl_sgen = p->shell_gen;
+  const bool stale = s->zl_edges != p->cached_edges || s->zl_dims != p->cached_dims || s->zl_f32 != p->cached_f32 ||
+                     s->zl_nsh != nsh || s->zl_sgen != p->shell_gen;   // the z-pass mode lists need rebuilding
+  // A pinned host field still to be read into the staging buffer ud: in row chunks overlapped with
+  // the set-up and the first batch's z pass when the mode lists are current and u advects itself,
+  // else in one piece first.
+  const void* hsrc = p->kept_src;
+  const int eb = p->io_f64 ? 16 : 8;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  FIT_CUDA_CHECK(cudaStreamIsCapturing(p->stream, &cap));
+  if (hsrc && !s->cs && cap == cudaStreamCaptureStatusNone) {   // the read stream and its events, once
+    // 16 chunks on 38 blocks of 256 threads (4 loads of 16 bytes each in flight): 512^3 host calls
+    // 84.5 -> 81.0 ms (8 chunks 81.1, 4 chunks 81.5; 76 blocks 81.4; a higher stream priority for
+    // the read changed nothing)
+    const char* ec = getenv("FIT_HOST_READ_CHUNKS");
+    int nch = ec ? atoi(ec) : 16;
+    nch = nch < 1 ? 1 : (nch > 64 ? 64 : nch);
+    const char* ebk = getenv("FIT_HOST_READ_BLOCKS");
+    s->cblocks = ebk ? atoi(ebk) : 38;
+    FIT_CUDA_CHECK(cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking));
+    FIT_CUDA_CHECK(cudaEventCreateWithFlags(&s->cfork, cudaEventDisableTiming));
+    s->cev.resize(nch);
+    for (int j = 0; j < nch; ++j) FIT_CUDA_CHECK(cudaEventCreateWithFlags(&s->cev[j], cudaEventDisableTiming));
   }
+  const bool pipe = hsrc && s->cs && s->cev.size() > 1 && !stale && ad == ud;
+  if (hsrc && !pipe) FIT_TRY(copy_kept_box(hsrc, (void*)ud, g.N, p->M, eb, p->stream));
   FzArgs a;
   memset(&a, 0, sizeof(a));
   a.K = K;
@@ -519,14 +527,110 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
   a.zent = (const uint16_t*)s->zent.p;
   a.ntile = ntile;
   const float2* tw = p->ax[0].tw32;
+  auto fill_batch = [&](size_t b0) {
+    a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
+    for (int b = 0; b < a.nb; ++b) {
+      a.med[b] = meds[b0 + b];
+      for (int d = 0; d < 3; ++d) {   // the mediator's extent in live-box units (never beyond K)
+        const int e = s->ext[3 * (a.med[b] - 1) + d];
+        a.ext[b][d] = (short)(e < K ? e : K);
+      }
+    }
+  };
+  auto setup = [&](long c0, long c1) -> int {   // H, carrier and shell maps of pencils [c0, c1)
+    if (c1 <= c0) return FIT_OK;
+    const long n = (c1 - c0) * KY;
+    fit_prof_begin(PK_CARRIER, (double)n * (2 * 6 * 16 + 6 * 8 + 4), p->stream);
+    if (p->io_f64)
+      k_fz_setup<double><<<(unsigned)((n + 255) / 256), 256, 0, p->stream>>>(
+          g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se,
+          sbp, -1, nullptr, P1S, c0, c1 - c0);
+    else
+      k_fz_setup<float><<<(unsigned)((n + 255) / 256), 256, 0, p->stream>>>(
+          g, p->kt, K, KX, KY, P1, ud, p->io_f64, inv, p->dealias == 1, (const uint16_t*)p->shell_full.p, H, Ce, se,
+          sbp, -1, nullptr, P1S, c0, c1 - c0);
+    fit_prof_end(p->stream);
+    FIT_LAUNCH_CHECK();
+    return FIT_OK;
+  };
+  auto zinv = [&](int t0, int t1) -> int {   // the first batch's z pass over pencil tiles [t0, t1)
+    if (t1 <= t0) return FIT_OK;
+    int rc = fz_zinv_a(M, a, H, (const float*)s->fkd.p, (float2*)s->fA.p, tw, t0, t1, p->stream);
+    if (rc == 1) rc = fz_zinv_b(M, a, H, (const float*)s->fkd.p, (float2*)s->fA.p, tw, t0, t1, p->stream);
+    if (rc == 1) fit_set_error("no fused kernels for size %d", M);
+    return rc == 1 ? FIT_ERR_SIZE : rc;
+  };
+  fill_batch(0);
+  // Chunk j holds the live rows ky' = K + f with |f| in [y_j, y_{j+1}) (y_0 = 0, y_nch = K + 1): its
+  // field rows are read (both signs: the set-up pairs k with -k), then its pencils set up, then the
+  // first batch's z pass runs over the tiles of C pencils that lie wholly in the rows set up so far.
+  const int nch = pipe ? (int)s->cev.size() : 1;
+  if (pipe) {
+    FIT_CUDA_CHECK(cudaEventRecord(s->cfork, p->stream));
+    FIT_CUDA_CHECK(cudaStreamWaitEvent(s->cs, s->cfork, 0));
+    for (int j = 0; j < nch; ++j) {
+      const int ya = (int)((long)j * (K + 1) / nch), yb = (int)((long)(j + 1) * (K + 1) / nch);
+      FIT_TRY(copy_kept_rows(hsrc, (void*)ud, g.N, p->M, eb, ya, yb, s->cblocks, s->cs));
+      FIT_CUDA_CHECK(cudaEventRecord(s->cev[j], s->cs));
+    }
+  }
+  int cl = 0, ch = 0;   // tiles [cl, ch) have had their z pass (empty while ch == cl)
+  for (int j = 0; j < nch; ++j) {
+    const int ya = (int)((long)j * (K + 1) / nch), yb = (int)((long)(j + 1) * (K + 1) / nch);
+    if (pipe) FIT_CUDA_CHECK(cudaStreamWaitEvent(p->stream, s->cev[j], 0));
+    if (ya == 0) {
+      FIT_TRY(setup((long)(K - yb + 1) * KX, (long)(K + yb) * KX));
+    } else {
+      FIT_TRY(setup((long)(K - yb + 1) * KX, (long)(K - ya + 1) * KX));
+      FIT_TRY(setup((long)(K + ya) * KX, (long)(K + yb) * KX));
+    }
+    if (j == nch - 1 && stale) {   // shell table changed: rebuild the z-pass mode lists (an eager call)
+      const long nmodes = nset, nl = (long)nsh * ntile;
+      FIT_TRY(ensure(p, &s->zoff, sizeof(unsigned) * (size_t)(nl + 1)));
+      FIT_TRY(ensure(p, &s->zfill, sizeof(unsigned) * (size_t)nl));
+      FIT_TRY(ensure(p, &s->zent, sizeof(uint16_t) * (size_t)nmodes));
+      FIT_CUDA_CHECK(cudaMemsetAsync(s->zfill.p, 0, sizeof(unsigned) * (size_t)nl, p->stream));
+      const unsigned gb = (unsigned)((nmodes + 255) / 256);
+      k_zl_count<<<gb, 256, 0, p->stream>>>(sbp, nmodes, P1, C, ntile, (unsigned*)s->zfill.p);
+      FIT_LAUNCH_CHECK();
+      k_zl_scan<<<1, 1024, 0, p->stream>>>((const unsigned*)s->zfill.p, nl, (unsigned*)s->zoff.p);
+      FIT_LAUNCH_CHECK();
+      FIT_CUDA_CHECK(cudaMemsetAsync(s->zfill.p, 0, sizeof(unsigned) * (size_t)nl, p->stream));
+      k_zl_fill<<<gb, 256, 0, p->stream>>>(sbp, nmodes, P1, C, ntile, (const unsigned*)s->zoff.p, (unsigned*)s->zfill.p,
+                                           (uint16_t*)s->zent.p);
+      FIT_LAUNCH_CHECK();
+      s->zl_edges = p->cached_edges;
+      s->zl_dims = p->cached_dims;
+      s->zl_f32 = p->cached_f32;
+      s->zl_nsh = nsh;
+      s->zl_sgen = p->shell_gen;
+      a.zoff = (const unsigned*)s->zoff.p;
+      a.zent = (const uint16_t*)s->zent.p;
+    }
+    const long lo = (long)(K - yb + 1) * KX, hi = (long)(K + yb) * KX;   // pencils set up so far
+    const int tl = (int)((lo + C - 1) / C), th = hi >= P1 ? ntile : (int)(hi / C);
+    if (tl < th) {
+      if (ch == cl) {
+        FIT_TRY(zinv(tl, th));
+      } else {
+        FIT_TRY(zinv(tl, cl));
+        FIT_TRY(zinv(ch, th));
+      }
+      cl = tl;
+      ch = th;
+    }
+  }
   // advecting velocity in physical space (once per call), its unnormalised inverse transform scaled
   // by 1/Mtot^2: the x pass multiplies it by the unnormalised inverse transforms of the gradients,
-  // so that product carries both transforms' 1/Mtot without a per-element rescale
+  // so that product carries both transforms' 1/Mtot without a per-element rescale. Its scratch is
+  // the y-pass buffer, unused until the first batch's y pass.
   const double usc = 1.0 / ((double)g.Mtot * (double)g.Mtot);
   if (ad == ud) {   // self-advection: H already holds its live box
     const float sc = (float)usc;
-    int rc = fz_velocity_a(M, a, H, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p, tw, sc, p->stream);
-    if (rc == 1) rc = fz_velocity_b(M, a, H, (float2*)s->fA.p, (float2*)s->fB.p, (float*)p->ph.p, tw, sc, p->stream);
+    float2* vz = (float2*)s->fB.p;
+    float2* vy = vz + 3L * M * P1;
+    int rc = fz_velocity_a(M, a, H, vz, vy, (float*)p->ph.p, tw, sc, p->stream);
+    if (rc == 1) rc = fz_velocity_b(M, a, H, vz, vy, (float*)p->ph.p, tw, sc, p->stream);
     if (rc != FIT_OK) return rc == 1 ? FIT_ERR_SIZE : rc;
   } else {
     FIT_TRY(ensure(p, &p->hs, sizeof(float2) * 3 * g.Mhalf));
@@ -545,14 +649,8 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     FIT_TRY(inverse_nd<float>((float2*)p->hs.p, (float*)p->ph.p, g, p->ax, 3, (float)usc, p->stream));
   }
   for (size_t b0 = 0; b0 < meds.size(); b0 += B) {
-    a.nb = (int)((meds.size() - b0) < (size_t)B ? (meds.size() - b0) : (size_t)B);
-    for (int b = 0; b < a.nb; ++b) {
-      a.med[b] = meds[b0 + b];
-      for (int d = 0; d < 3; ++d) {   // the mediator's extent in live-box units (never beyond K)
-        const int e = s->ext[3 * (a.med[b] - 1) + d];
-        a.ext[b][d] = (short)(e < K ? e : K);
-      }
-    }
+    fill_batch(b0);
+    a.nozinv = b0 == 0;   // the first batch's z pass ran above
     int rc = fz_dispatch_a(M, a, H, Ce, se, (const float*)s->fkd.p, (const float*)p->ph.p, (float2*)s->fA.p,
                            (float2*)s->fB.p, (double*)s->fpart.p, tw, (int*)s->ferr.p, p->stream);
     if (rc == 1)
@@ -907,7 +1005,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
   // output, the shell set and every workspace allocation are unchanged.
   const bool same = s->key_u == ud && s->key_a == ad && s->key_inv == inv && s->key_edges == p->cached_edges &&
                     s->key_dims == p->cached_dims && s->key_f32 == p->cached_f32 && s->key_T == Td &&
-                    s->key_gen == p->buf_gen && s->key_sgen == p->shell_gen;
+                    s->key_gen == p->buf_gen && s->key_sgen == p->shell_gen && s->key_h == p->kept_src;
   if (!same) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
     s->exec = nullptr;
@@ -944,6 +1042,7 @@ int s2s_batched(fit_plan* p, const void* ud, const void* ad, int inv, double* Td
     s->key_T = Td;
     s->key_gen = p->buf_gen;
     s->key_sgen = p->shell_gen;
+    s->key_h = p->kept_src;
     return FIT_OK;
   }
   if (fit_prof_on()) {   // per-launch events need eager launches

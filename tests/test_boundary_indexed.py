@@ -64,25 +64,41 @@ def test_set_shell_index_rejects_out_of_range():
         plan.shell_to_shell_indexed(u, 4, 0, F._lib.S2S_PLAIN)
 
 
-@pytest.mark.parametrize("n,copy_engine", [(64, False), (64, True), (96, False)])
-def test_pinned_host_input_kept_box(n, copy_engine, monkeypatch):
+@pytest.mark.parametrize("n,copy_engine,f64,chunks", [(64, False, False, None), (64, True, False, None),
+                                                      (96, False, False, None), (64, False, True, None),
+                                                      (96, False, False, (5, 3))])
+def test_pinned_host_input_kept_box(n, copy_engine, f64, chunks, monkeypatch):
     """Host-pointer call of the batched 2/3 form: pinned host memory is read by the device over the
-    host link (only the kept box, in 16-byte pairs with single elements at odd run ends: 64 has an
-    odd first run, 96 an odd start of the second), or through the copy engines; both match the
-    oracle."""
+    host link (only the kept box; complex64 in 16-byte pairs with single elements at odd run ends: 64
+    has an odd first run, 96 an odd start of the second; complex128 element by element), or through
+    the copy engines; both match the oracle. From the second call on (mode lists current) the read
+    runs in chunks of y rows beside the set-up and the first z pass (`chunks`: a chunk count that does
+    not divide K + 1, on a 3-block grid); the replayed graph reads the host buffer afresh, so a new
+    field written into it gives that field's matrix."""
     torch = pytest.importorskip("torch")
     if copy_engine:
         monkeypatch.setenv("FIT_KEPT_BOX_COPY_ENGINE", "1")
+    if chunks:
+        monkeypatch.setenv("FIT_HOST_READ_CHUNKS", str(chunks[0]))
+        monkeypatch.setenv("FIT_HOST_READ_BLOCKS", str(chunks[1]))
     ns = (n, n, n)
-    u, ks = spectrum_field(ns, e_config2, seed=9)
-    pinned = torch.empty((3, n, n, n), dtype=torch.complex64, pin_memory=True)
+    ct = torch.complex128 if f64 else torch.complex64
+    pinned = torch.empty((3, n, n, n), dtype=ct, pin_memory=True)
     host = np.transpose(pinned.numpy(), (3, 2, 1, 0))     # column-major (n, n, n, 3) view
-    host[...] = u.astype(np.complex64)
-    plan = Plan(ns, 3, 3, "two_thirds", 32, False, ks)
+    u, ks = spectrum_field(ns, e_config2, seed=9)
+    host[...] = u.astype(host.dtype)
+    plan = Plan(ns, 3, 3, "two_thirds", 32, f64, ks)
     _, edges, Tref, _, _ = O.shell_to_shell(host.astype(np.complex128), ks, ("linear", 6.0), "two_thirds")
     before = plan.info()[8]
     for _ in range(3):
         T, _, _ = plan.shell_to_shell(host, edges, 7, 0, 0, F._lib.S2S_BATCHED)
         assert np.max(np.abs(T - Tref)) <= 1e-5 * np.max(np.abs(Tref))
     K = n // 3 - 1
-    assert plan.info()[8] - before == 3 * 3 * (2 * K + 1) ** 3 * 8   # only the kept box travels
+    eb = 16 if f64 else 8
+    assert plan.info()[8] - before == 3 * 3 * (2 * K + 1) ** 3 * eb   # only the kept box travels
+    u2, _ = spectrum_field(ns, e_config2, seed=10)
+    host[...] = u2.astype(host.dtype)
+    _, _, Tref2, _, _ = O.shell_to_shell(host.astype(np.complex128), ks, ("linear", 6.0), "two_thirds")
+    T2, _, _ = plan.shell_to_shell(host, edges, 7, 0, 0, F._lib.S2S_BATCHED)
+    assert np.max(np.abs(T2 - Tref2)) <= 1e-5 * np.max(np.abs(Tref2))
+    assert np.max(np.abs(Tref2 - Tref)) > 1e-3 * np.max(np.abs(Tref))
