@@ -109,7 +109,10 @@ int fit_spectral_flux(fit_plan* plan, const void* u_hat, const void* adv_hat, co
  * → _shell_to_shell_fft! (ext/FlowInvariantTransferFFTWExt.jl:209-295) and the GPU/threaded
  * execution backends (ext/FlowInvariantTransferKernelAbstractionsExt.jl:68-138,
  * ext/FlowInvariantTransferOhMyThreadsExt.jl:24-97). mode = FIT_S2S_PLAIN or FIT_S2S_BATCHED.
- * max_asym receives NaN when verify = 0. */
+ * max_asym receives NaN when verify = 0. Host arguments of the batched form on a 2/3 plan of a
+ * fused transform size: only the 2/3-kept box of u_hat is read; page-locked host memory is read
+ * by the device during the step (overlapped with its first passes), other host memory is copied
+ * before it. */
 int fit_shell_to_shell(fit_plan* plan, const void* u_hat, const void* adv_hat, const double* edges, int n_edges,
                        uint32_t dims_mask, int coord_f32, int invariant, int mode, int verify, double* T_colmajor,
                        double* net, double* max_asym, int ptr_kind);
