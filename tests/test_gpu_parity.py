@@ -135,6 +135,36 @@ def test_scalar_flux_and_decomposed_flux():
         assert rel(rh[name].transfer_spectrum, T) < 1e-11
 
 
+@pytest.mark.parametrize("field", ["reference", "solenoidal"])
+def test_execution_forms_agree(field):     # runtests.jl:993-1023
+    """The reference's serial/threaded/distributed parity check: the plain and batched FP64 forms
+    agree to 1e-12 (absolute on its field, u = (cos x, cos y) on 8^2, whose transfer the 2/3 rule
+    removes entirely; relative to max|T| on a random solenoidal 16^2 field), as its execution
+    backends do, and both equal the oracle; the batched FP32 form is within FP32 rounding.
+    LinearBinning(1), 2/3 rule."""
+    if field == "reference":
+        N = 8
+        ks = F.wavenumber_grid((N, N), (2 * np.pi,) * 2)
+        u = np.zeros((N, N, 2), complex)
+        u[1, 0, 0] = u[N - 1, 0, 0] = 0.5
+        u[0, 1, 1] = u[0, N - 1, 1] = 0.5
+    else:
+        u, ks = solenoidal_2d(16, 17)
+    b = F.LinearBinning(1.0)
+    r = {(p, m): F.calculate_shell_to_shell_transfer(u, ks, binning=b, spectral=F.GB300Spectral(p),
+                                                     execution=F.GB300Execution(m))
+         for p, m in ((64, "plain"), (64, "batched"), (32, "batched"))}
+    _, _, T, net, _ = O.shell_to_shell(u, ks, ("linear", 1.0), "two_thirds")
+    scale = max(np.abs(T).max(), 1.0) if field == "reference" else np.abs(T).max()
+    assert field == "reference" or scale > 0
+    a, c = r[(64, "plain")], r[(64, "batched")]
+    assert np.max(np.abs(a.transfer_matrix - c.transfer_matrix)) <= 1e-12 * scale
+    assert np.max(np.abs(a.net_transfer - c.net_transfer)) <= 1e-12 * scale
+    assert np.max(np.abs(a.transfer_matrix - T)) <= 1e-12 * scale
+    assert np.max(np.abs(a.net_transfer - net)) <= 1e-12 * scale
+    assert np.max(np.abs(r[(32, "batched")].transfer_matrix - T)) <= 1e-5 * scale
+
+
 @pytest.mark.parametrize("prec", [64, 32])
 @pytest.mark.parametrize("mode", ["plain", "batched"])
 @pytest.mark.parametrize("deal", ["none", "two_thirds", "three_halves"])
