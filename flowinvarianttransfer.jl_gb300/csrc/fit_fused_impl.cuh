@@ -1312,7 +1312,7 @@ int fz_zinv_tiles(const FzArgs& a, const float2* H, const float* kd, float2* buf
   typedef FzTile<N> TT;
   const size_t sm = TT::SMEM;
   FIT_TRY(ct_prep_fused(k_fz_zinv<N>, sm, TT::NTHR));
-  if (t1 <= t0) return FIT_OK;
+  if (t1 <= t0 || a.nb < 1) return FIT_OK;
   const int pt = (int)((a.P1 + TT::C - 1) / TT::C);
   double zin_b = 0.0;   // the tile range's share of the batch's algorithmic bytes (as in fz_batch)
   for (int b = 0; b < a.nb; ++b) {

@@ -554,7 +554,7 @@ static int run_fused(fit_plan* p, S2SState* s, const void* ud, const void* ad, i
     return FIT_OK;
   };
   auto zinv = [&](int t0, int t1) -> int {   // the first batch's z pass over pencil tiles [t0, t1)
-    if (t1 <= t0) return FIT_OK;
+    if (t1 <= t0 || a.nb < 1) return FIT_OK;   // no mediator holds a kept mode: nothing to transform
     int rc = fz_zinv_a(M, a, H, (const float*)s->fkd.p, (float2*)s->fA.p, tw, t0, t1, p->stream);
     if (rc == 1) rc = fz_zinv_b(M, a, H, (const float*)s->fkd.p, (float2*)s->fA.p, tw, t0, t1, p->stream);
     if (rc == 1) fit_set_error("no fused kernels for size %d", M);

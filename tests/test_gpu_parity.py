@@ -395,3 +395,22 @@ def test_fused_shell_to_shell_conservation_floor(seed):
     assert res[64][1] < 1e-12
     assert res[32][1] < 3e-7
     assert rel(res[32][0], res[64][0]) < 1e-5
+
+
+def test_fused_shell_to_shell_shells_without_kept_modes():
+    """Shells that hold no mode of the 2/3-kept box (64^3: kept |k_d| <= 20, so |k| <= 34.7) leave no
+    mediator for the fused batched form, and every T(n, m) is a sum over no triad: eager, captured
+    and replayed calls, from a host array and from a pinned host buffer, return all zeros."""
+    torch = pytest.importorskip("torch")
+    F.clear_plans()
+    n = 64
+    u, ks = spectrum_field((n, n, n), e_config2, seed=4)
+    edges = np.array([40.0, 45.0, 50.0])
+    plan = F.Plan((n, n, n), 3, 3, "two_thirds", 32, False, ks)
+    pinned = torch.empty((3, n, n, n), dtype=torch.complex64, pin_memory=True)
+    host = np.transpose(pinned.numpy(), (3, 2, 1, 0))
+    host[...] = u.astype(np.complex64)
+    for arr in (np.asfortranarray(u.astype(np.complex64)), host):
+        for _ in range(3):
+            T, net, _ = plan.shell_to_shell(arr, edges, 7, 0, 0, F._lib.S2S_BATCHED)
+            assert T.shape == (2, 2) and not np.any(T) and not np.any(net)
