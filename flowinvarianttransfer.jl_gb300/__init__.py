@@ -6,8 +6,8 @@ built on it — spectral flux, shell-to-shell, partial fluxes, mode-to-mode — 
 coarse-graining flux, a forced Navier-Stokes evolver and the learned subfilter-stress closure.
 """
 from .types import *  # noqa: F401,F403
-from .shells import (wavenumber_grid, shell_edges, shell_centers, n_shells, default_binning, kmax,  # noqa: F401
-                     dims_mask)
+from .shells import (wavenumber_grid, wavenumber_magnitude_grid, dealiasing_mask, shell_edges,  # noqa: F401
+                     shell_centers, n_shells, default_binning, kmax, dims_mask)
 from .api import (compute_nonlinear_term, transfer_density, decompose_field, assign_shells_device,  # noqa: F401
                   calculate_spectral_flux, calculate_scalar_flux, calculate_shell_to_shell_transfer,
                   calculate_scalar_shell_to_shell_transfer, calculate_partial_fluxes,

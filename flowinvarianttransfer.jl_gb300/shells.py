@@ -28,6 +28,48 @@ def wavenumber_grid(ns, Ls):
     return tuple(out)
 
 
+def wavenumber_magnitude_grid(ks):
+    """|k| at every point of the grid spanned by ``ks`` (``src/Utils.jl:76-88``): an array of shape
+    (len(ks[0]), ..., len(ks[D-1])) in the promoted element type of ``ks`` (Float32 wavenumbers give
+    Float32 magnitudes), the squares summed in dimension order from zero and the square root taken
+    once, as the reference does."""
+    ks = [np.asarray(k) for k in ks]
+    ft = np.result_type(*[k.dtype for k in ks])
+    D = len(ks)
+    s = np.zeros(tuple(len(k) for k in ks), dtype=ft)
+    for d, k in enumerate(ks):
+        shape = [1] * D
+        shape[d] = len(k)
+        kk = k.astype(ft, copy=False).reshape(shape)
+        s = s + kk * kk
+    return np.sqrt(s)
+
+
+def dealiasing_mask(ns, rule="twothirds", out=None):
+    """Keep/discard mask of grid shape ``ns`` (``dealiasing_mask`` / ``dealiasing_mask!``,
+    ``src/Utils.jl:110-138``): True where every axis keeps its mode, i.e. the FFTW-order index's
+    ``|k_d| = min(i, N_d - i)`` is below ``N_d * threshold``; threshold 1/3 for ``rule="twothirds"``,
+    else 1/2. The threshold is the reference's floating-point one (``N/3``, so N = 64 keeps
+    ``|k| <= 21``), not the integer ``N div 3`` cut of the nonlinear term's dealiasing. With ``out``
+    (a boolean array of shape ``ns``) the mask is written there and ``out`` returned, as the
+    in-place form does."""
+    ns = tuple(int(n) for n in ns)
+    threshold = 1.0 / 3.0 if rule == "twothirds" else 0.5
+    keep = np.ones(ns, dtype=bool)
+    for d, N in enumerate(ns):
+        idx = np.arange(N)
+        kabs = np.where(idx <= N // 2, idx, N - idx)
+        shape = [1] * len(ns)
+        shape[d] = N
+        keep &= (kabs < N * threshold).reshape(shape)
+    if out is None:
+        return keep
+    if out.shape != ns:
+        raise ValueError(f"mask has shape {out.shape}; expected {ns}")
+    out[...] = keep
+    return out
+
+
 def dims_of(geometry, nd):
     dims = tuple(range(1, nd + 1)) if geometry is None or geometry.dims is None else tuple(geometry.dims)
     if not all(1 <= d <= nd for d in dims):
